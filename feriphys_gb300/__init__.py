@@ -1,0 +1,412 @@
+"""feriphys_gb300 -- GB300-native spring-mass-damper cloth step.
+
+A Python mirror of feriphys's springy-simulation API over the C ABI in
+include/feriphys_gb300.h (libferiphys_gb300.so, hand-written CUDA for
+sm_103a).  Names follow the reference (file:line relative to its root):
+
+    Cloth.new            springy/cloth.rs:20-113
+    SpringyMesh.new      springy/springy_mesh.rs:267-401  (+ add_strut, add_pin,
+                         get_points, get_vertices, accumulate_forces,
+                         update_points, clear_forces)
+    CollidableMesh.new   collidable_mesh.rs:57-97
+    Simulation.new       springy/simulation.rs:17-25      (+ step, get_timestep,
+                         get_meshes, get_obstacles, set_config)
+    Config, Integration  springy/config.rs:9-33, state.rs:4-8
+
+There is no CPU fallback: importing the package loads the CUDA library (it is
+built first when missing or stale and nvcc is available) and raises if it
+cannot.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Integration", "Config", "SpringyMesh", "Cloth", "CollidableMesh", "Simulation", "FgbError",
+           "library_path", "POINT_FIELDS"]
+
+POINT_FIELDS = ("mass", "px", "py", "pz", "vx", "vy", "vz", "fx", "fy", "fz")
+
+
+class FgbError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__("fgb error %d: %s" % (code, message))
+        self.code = code
+
+
+class Integration(enum.IntEnum):
+    Euler = 0
+    Rk4 = 1
+
+
+class Config(C.Structure):
+    """springy/config.rs Config.  gravity is a force per point (not m*g)."""
+
+    _fields_ = [
+        ("integration", C.c_int32),
+        ("dt", C.c_float),
+        ("gravity", C.c_float * 3),
+        ("wind", C.c_float * 3),
+        ("lift_coefficient", C.c_float),
+        ("drag_coefficient", C.c_float),
+        ("coefficient_of_restitution", C.c_float),
+        ("coefficient_of_friction", C.c_float),
+    ]
+
+    @classmethod
+    def default(cls) -> "Config":
+        c = cls()
+        _check(_lib().fgb_config_default(C.byref(c)))
+        return c
+
+    @classmethod
+    def make(cls, integration=Integration.Euler, dt=1e-3, gravity=(0.0, -10.0, 0.0), wind=(0.0, 0.0, 0.0),
+             lift_coefficient=1.0, drag_coefficient=1.0, coefficient_of_restitution=0.95,
+             coefficient_of_friction=0.3) -> "Config":
+        c = cls()
+        c.integration = int(integration)
+        c.dt = float(dt)
+        c.gravity[:] = [float(v) for v in gravity]
+        c.wind[:] = [float(v) for v in wind]
+        c.lift_coefficient = float(lift_coefficient)
+        c.drag_coefficient = float(drag_coefficient)
+        c.coefficient_of_restitution = float(coefficient_of_restitution)
+        c.coefficient_of_friction = float(coefficient_of_friction)
+        return c
+
+
+class _Override(C.Structure):
+    _fields_ = [("a", C.c_uint32), ("b", C.c_uint32), ("stiffness", C.c_float), ("damping", C.c_float)]
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def _declare(l):
+    P, U64, U32, F, I = C.c_void_p, C.c_uint64, C.c_uint32, C.c_float, C.c_int
+    pp = C.POINTER(C.c_void_p)
+    cfg = C.POINTER(Config)
+    sig = {
+        "fgb_last_error": (C.c_char_p, []),
+        "fgb_config_default": (I, [cfg]),
+        "fgb_mesh_new": (I, [P, U64, P, U64, F, F, F, P, U64, pp]),
+        "fgb_cloth_new": (I, [U64, U64, F, P, F, F, F, F, F, F, F, P, U64, pp]),
+        "fgb_mesh_add_strut": (I, [P, U32, U32, F, F]),
+        "fgb_mesh_add_pin": (I, [P, U32]),
+        "fgb_mesh_counts": (I, [P, P]),
+        "fgb_mesh_get_struts": (I, [P, P, P]),
+        "fgb_mesh_set_strut_params": (I, [P, P, P]),
+        "fgb_mesh_get_points": (I, [P, P]),
+        "fgb_mesh_set_points": (I, [P, P]),
+        "fgb_mesh_get_positions": (I, [P, P]),
+        "fgb_mesh_get_points_f64": (I, [P, P]),
+        "fgb_mesh_get_vertices": (I, [P, P, P]),
+        "fgb_mesh_set_path": (I, [P, I]),
+        "fgb_mesh_get_path": (I, [P, C.POINTER(C.c_int)]),
+        "fgb_mesh_set_precision": (I, [P, I]),
+        "fgb_mesh_accumulate_forces": (I, [P, cfg]),
+        "fgb_mesh_integrate": (I, [P, C.c_int32, F]),
+        "fgb_mesh_update_points": (I, [P, P, U64, cfg]),
+        "fgb_mesh_clear_forces": (I, [P]),
+        "fgb_mesh_synchronize": (I, [P]),
+        "fgb_mesh_destroy": (I, [P]),
+        "fgb_collidable_new": (I, [P, U64, P, U64, pp]),
+        "fgb_collidable_counts": (I, [P, P]),
+        "fgb_collidable_destroy": (I, [P]),
+        "fgb_sim_new": (I, [P, U64, P, U64, pp]),
+        "fgb_sim_set_config": (I, [P, cfg]),
+        "fgb_sim_get_config": (I, [P, cfg]),
+        "fgb_sim_step": (I, [P, U64]),
+        "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
+        "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
+        "fgb_sim_destroy": (I, [P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        try:
+            path = _build.build()
+        except RuntimeError as e:  # no nvcc: use a prebuilt library if there is one
+            if not os.path.exists(path):
+                raise ImportError("libferiphys_gb300.so is missing and cannot be built: %s" % e) from None
+        l = C.CDLL(path)
+        _declare(l)
+        _LIB = l
+    return _LIB
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise FgbError(rc, _lib().fgb_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1))
+
+
+def _u32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32).reshape(-1))
+
+
+class SpringyMesh:
+    """A GPU-backed springy mesh (springy_mesh.rs:258-661)."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def new(cls, vertex_positions, vertex_indices, mass, default_stiffness, default_damping,
+            strut_overrides=None) -> "SpringyMesh":
+        """SpringyMesh::new.  strut_overrides: {(a, b): (stiffness, damping)} or
+        a pair of arrays (pairs[n, 2], kc[n, 2]), or None."""
+        pos = _f32(vertex_positions)
+        idx = _u32(vertex_indices)
+        ov = None
+        nov = 0
+        if strut_overrides is not None:
+            if isinstance(strut_overrides, dict):
+                items = list(strut_overrides.items())
+                pairs = np.array([k for k, _ in items], np.uint32).reshape(-1, 2)
+                kc = np.array([v for _, v in items], np.float32).reshape(-1, 2)
+            else:
+                pairs = np.asarray(strut_overrides[0], np.uint32).reshape(-1, 2)
+                kc = np.asarray(strut_overrides[1], np.float32).reshape(-1, 2)
+            nov = len(pairs)
+            ov = (_Override * max(1, nov))()
+            arr = np.ctypeslib.as_array(C.cast(ov, C.POINTER(C.c_uint32)), shape=(max(1, nov) * 4,))
+            rec = arr.view(np.uint32).reshape(-1, 4)[:nov]
+            rec[:, 0:2] = pairs
+            rec[:, 2:4] = kc.view(np.uint32)
+        h = C.c_void_p()
+        _check(_lib().fgb_mesh_new(_ptr(pos), pos.size // 3, _ptr(idx), idx.size, float(mass),
+                                   float(default_stiffness), float(default_damping),
+                                   C.cast(ov, C.c_void_p) if ov is not None else None, nov, C.byref(h)))
+        return cls(h.value)
+
+    def __del__(self):
+        try:
+            if self._h and _LIB is not None:
+                _LIB.fgb_mesh_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def add_strut(self, vertex_indices, stiffness, damping):
+        a, b = vertex_indices
+        _check(_lib().fgb_mesh_add_strut(self._h, int(a), int(b), float(stiffness), float(damping)))
+
+    def add_pin(self, pin_index):
+        _check(_lib().fgb_mesh_add_pin(self._h, int(pin_index)))
+
+    def counts(self):
+        out = np.zeros(4, np.uint64)
+        _check(_lib().fgb_mesh_counts(self._h, _ptr(out)))
+        return tuple(int(v) for v in out)
+
+    @property
+    def n_points(self) -> int:
+        return self.counts()[0]
+
+    def get_points(self, out=None) -> np.ndarray:
+        """Points as [n, 10] float32 in the Stateful::as_state layout."""
+        n = self.n_points
+        if out is None:
+            out = np.empty((n, 10), np.float32)
+        _check(_lib().fgb_mesh_get_points(self._h, _ptr(out)))
+        return out
+
+    def get_points_f64(self) -> np.ndarray:
+        out = np.empty((self.n_points, 10), np.float64)
+        _check(_lib().fgb_mesh_get_points_f64(self._h, _ptr(out)))
+        return out
+
+    def set_points(self, points):
+        """Stateful::from_state_vector for every point ([n, 10] float32)."""
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        if pts.size != 10 * self.n_points:
+            raise ValueError("expected %d floats" % (10 * self.n_points))
+        _check(_lib().fgb_mesh_set_points(self._h, _ptr(pts)))
+
+    def get_positions(self) -> np.ndarray:
+        out = np.empty((self.n_points, 3), np.float32)
+        _check(_lib().fgb_mesh_get_positions(self._h, _ptr(out)))
+        return out
+
+    def get_vertices(self):
+        """SpringyMesh::get_vertices: (positions [n, 3], indices [3F])."""
+        n, _, f, _ = self.counts()
+        pos = np.empty((n, 3), np.float32)
+        idx = np.empty(3 * f, np.uint32)
+        _check(_lib().fgb_mesh_get_vertices(self._h, _ptr(pos), _ptr(idx)))
+        return pos, idx
+
+    def get_struts(self):
+        """(kcl [S, 3]: stiffness, damping, rest length; ab [S, 2])."""
+        s = self.counts()[1]
+        kcl = np.empty((s, 3), np.float32)
+        ab = np.empty((s, 2), np.uint32)
+        _check(_lib().fgb_mesh_get_struts(self._h, _ptr(kcl), _ptr(ab)))
+        return kcl, ab
+
+    def set_strut_params(self, stiffness, damping):
+        k = _f32(stiffness)
+        c = _f32(damping)
+        if k.size != self.counts()[1] or c.size != k.size:
+            raise ValueError("one stiffness and damping per strut expected")
+        _check(_lib().fgb_mesh_set_strut_params(self._h, _ptr(k), _ptr(c)))
+
+    def set_path(self, path: int):
+        _check(_lib().fgb_mesh_set_path(self._h, int(path)))
+
+    def get_path(self) -> int:
+        p = C.c_int()
+        _check(_lib().fgb_mesh_get_path(self._h, C.byref(p)))
+        return p.value
+
+    def set_precision(self, bits: int):
+        _check(_lib().fgb_mesh_set_precision(self._h, int(bits)))
+
+    # phase hooks of Simulation::step
+    def accumulate_forces(self, config: Config):
+        _check(_lib().fgb_mesh_accumulate_forces(self._h, C.byref(config)))
+
+    def integrate(self, integration, dt):
+        """State::euler_step / rk4_step into the mesh's staged points."""
+        _check(_lib().fgb_mesh_integrate(self._h, int(integration), float(dt)))
+
+    def update_points(self, obstacles, config: Config):
+        arr = (C.c_void_p * max(1, len(obstacles)))(*[o._h for o in obstacles])
+        _check(_lib().fgb_mesh_update_points(self._h, arr, len(obstacles), C.byref(config)))
+
+    def clear_forces(self):
+        _check(_lib().fgb_mesh_clear_forces(self._h))
+
+    def synchronize(self):
+        _check(_lib().fgb_mesh_synchronize(self._h))
+
+
+class Cloth:
+    """springy/cloth.rs Cloth: ``Cloth.new(...).mesh`` is a SpringyMesh."""
+
+    def __init__(self, mesh: SpringyMesh):
+        self.mesh = mesh
+
+    @classmethod
+    def new(cls, rows, cols, spacing, position, point_mass, tensile_stiffness, tensile_damping, shear_stiffness,
+            shear_damping, binding_spring_stiffness, binding_spring_damping, pinned_vertices=()) -> "Cloth":
+        p = _f32(position)
+        pins = _u32(pinned_vertices)
+        h = C.c_void_p()
+        _check(_lib().fgb_cloth_new(int(rows), int(cols), float(spacing), _ptr(p), float(point_mass),
+                                    float(tensile_stiffness), float(tensile_damping), float(shear_stiffness),
+                                    float(shear_damping), float(binding_spring_stiffness),
+                                    float(binding_spring_damping), _ptr(pins) if pins.size else None, pins.size,
+                                    C.byref(h)))
+        return cls(SpringyMesh(h.value))
+
+
+class CollidableMesh:
+    """collidable_mesh.rs CollidableMesh (static triangle obstacle)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def new(cls, vertex_positions, vertex_indices) -> "CollidableMesh":
+        pos = _f32(vertex_positions)
+        idx = _u32(vertex_indices)
+        h = C.c_void_p()
+        _check(_lib().fgb_collidable_new(_ptr(pos), pos.size // 3, _ptr(idx), idx.size, C.byref(h)))
+        return cls(h.value)
+
+    def counts(self):
+        out = np.zeros(3, np.uint64)
+        _check(_lib().fgb_collidable_counts(self._h, _ptr(out)))
+        return tuple(int(v) for v in out)
+
+    def __del__(self):
+        try:
+            if self._h and _LIB is not None:
+                _LIB.fgb_collidable_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class Simulation:
+    """springy/simulation.rs Simulation over GPU-backed meshes."""
+
+    def __init__(self, handle, meshes, obstacles):
+        self._h = C.c_void_p(handle)
+        self._meshes = list(meshes)  # the C simulation borrows these
+        self._obstacles = list(obstacles)
+
+    @classmethod
+    def new(cls, meshes, obstacles) -> "Simulation":
+        meshes = list(meshes)
+        obstacles = list(obstacles)
+        ma = (C.c_void_p * max(1, len(meshes)))(*[m._h for m in meshes])
+        oa = (C.c_void_p * max(1, len(obstacles)))(*[o._h for o in obstacles])
+        h = C.c_void_p()
+        _check(_lib().fgb_sim_new(ma, len(meshes), oa, len(obstacles), C.byref(h)))
+        return cls(h.value, meshes, obstacles)
+
+    def __del__(self):
+        try:
+            if self._h and _LIB is not None:
+                _LIB.fgb_sim_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def set_config(self, config: Config):
+        """Headless form of sync_sim_config_from_ui (simulation.rs:64-77)."""
+        _check(_lib().fgb_sim_set_config(self._h, C.byref(config)))
+
+    def get_config(self) -> Config:
+        c = Config()
+        _check(_lib().fgb_sim_get_config(self._h, C.byref(c)))
+        return c
+
+    def step(self, n_steps: int = 1) -> float:
+        """Simulation::step (n_steps times, queued asynchronously); returns the
+        simulated seconds of one step like the reference's Duration."""
+        _check(_lib().fgb_sim_step(self._h, int(n_steps)))
+        return self.get_timestep()
+
+    def get_timestep(self) -> float:
+        s = C.c_double()
+        _check(_lib().fgb_sim_get_timestep(self._h, C.byref(s)))
+        return s.value
+
+    def get_meshes(self):
+        return list(self._meshes)
+
+    def get_obstacles(self):
+        return list(self._obstacles)
+
+    def synchronize(self) -> bool:
+        """Wait for queued steps; True when a vertex went non-finite since the last call."""
+        bad = C.c_int()
+        _check(_lib().fgb_sim_synchronize(self._h, C.byref(bad)))
+        return bool(bad.value)

@@ -1,0 +1,859 @@
+// C ABI implementation (include/feriphys_gb300.h): handles, device memory,
+// streams and kernel launches.  Host-side construction lives in
+// mesh_build.cpp; the kernels in step_general.cu / step_grid.cu / state_io.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <set>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/feriphys_gb300.h"
+#include "kernels.h"
+#include "mesh_build.h"
+#include "physics.cuh"
+#include "state_io.h"
+
+using fgb::MeshTopo;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define FGB_CUDA(call)                                                                              \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return fail(FGB_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define FGB_CHECK_RC(expr)   \
+  do {                       \
+    int rc_ = (expr);        \
+    if (rc_ != FGB_OK) return rc_; \
+  } while (0)
+
+template <class P>
+void dfree(P*& p) {
+  if (p) cudaFree(reinterpret_cast<void*>(p));
+  p = nullptr;
+}
+
+template <class P>
+cudaError_t dalloc(P*& p, size_t bytes) {
+  dfree(p);
+  if (bytes == 0) bytes = 16;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  p = static_cast<P*>(q);
+  return e;
+}
+
+bool finite_nonneg(float x) { return std::isfinite(x) && x >= 0.0f; }
+
+}  // namespace
+
+struct fgb_obstacle {
+  uint64_t n_vertices = 0;
+  uint64_t n_edges = 0;
+  std::vector<fgb::ObsFace> faces;  // device layout, computed on the host
+};
+
+struct fgb_mesh {
+  MeshTopo topo;
+  int device = 0;
+  int path_req = 0;      // 0 auto, 1 general, 2 grid
+  int precision = 32;    // 32 or 64
+  int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
+  cudaStream_t stream = nullptr;
+
+  // host copy of the state while the device does not hold it (as_state layout)
+  std::vector<float> host_pts;
+  bool state_on_device = false;
+  bool topo_dirty = true;
+  bool pins_dirty = true;
+  bool csr_ready = false;
+
+  // device state
+  void* pos[2] = {nullptr, nullptr};
+  void* vel[2] = {nullptr, nullptr};
+  int cur = 0;
+  void* force = nullptr;
+  bool has_force = false;  // force buffer holds the points' accumulated force
+  void* spos = nullptr;
+  void* svel = nullptr;
+  void* sforce = nullptr;
+  bool staged = false;
+  float* d_io = nullptr;  // as_state staging (10 floats per point; doubles for f64 readback)
+  size_t d_io_bytes = 0;
+  uint8_t* d_pinned = nullptr;
+  unsigned* d_flags = nullptr;
+
+  // general topology
+  int* d_strut_off = nullptr;
+  int2* d_strut_inc = nullptr;
+  float4* d_strut_kcl = nullptr;
+  int* d_face_off = nullptr;
+  int* d_face_inc = nullptr;
+  int4* d_face_vtx = nullptr;
+  // grid topology
+  float4* d_grid = nullptr;
+
+  size_t elem() const { return precision == 64 ? sizeof(fgb::Dbl4) : sizeof(float4); }
+};
+
+struct fgb_sim {
+  std::vector<fgb_mesh*> meshes;
+  std::vector<fgb_obstacle*> obstacles;
+  fgb_config cfg;
+  fgb::ObsFace* d_faces = nullptr;
+  int n_faces = 0;
+};
+
+namespace {
+
+void init_host_state(fgb_mesh* m) {
+  const uint32_t n = m->topo.n;
+  m->host_pts.assign(10 * size_t(n), 0.0f);
+  for (uint32_t i = 0; i < n; ++i) {
+    float* p = &m->host_pts[10 * size_t(i)];
+    p[0] = m->topo.mass_per_vert;
+    p[1] = m->topo.pos[3 * size_t(i)];
+    p[2] = m->topo.pos[3 * size_t(i) + 1];
+    p[3] = m->topo.pos[3 * size_t(i) + 2];
+  }
+  m->state_on_device = false;
+}
+
+int ensure_stream(fgb_mesh* m) {
+  if (!m->stream) FGB_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  return FGB_OK;
+}
+
+int ensure_io(fgb_mesh* m, size_t bytes) {
+  if (m->d_io_bytes < bytes) {
+    FGB_CUDA(dalloc(m->d_io, bytes));
+    m->d_io_bytes = bytes;
+  }
+  return FGB_OK;
+}
+
+void free_state(fgb_mesh* m) {
+  for (int i = 0; i < 2; ++i) {
+    dfree(m->pos[i]);
+    dfree(m->vel[i]);
+  }
+  dfree(m->force);
+  dfree(m->spos);
+  dfree(m->svel);
+  dfree(m->sforce);
+  m->has_force = false;
+  m->staged = false;
+}
+
+void free_topology(fgb_mesh* m) {
+  dfree(m->d_strut_off);
+  dfree(m->d_strut_inc);
+  dfree(m->d_strut_kcl);
+  dfree(m->d_face_off);
+  dfree(m->d_face_inc);
+  dfree(m->d_face_vtx);
+  dfree(m->d_grid);
+  m->csr_ready = false;
+}
+
+// Device state -> host_pts (as_state layout, f32).
+int download_state(fgb_mesh* m) {
+  if (!m->state_on_device) return FGB_OK;
+  const int n = int(m->topo.n);
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * size_t(n)));
+  const void* F = m->has_force ? m->force : nullptr;
+  if (m->precision == 64)
+    FGB_CUDA((fgb::launch_pack_f32<double>(n, m->pos[m->cur], m->vel[m->cur], F, m->d_io, m->stream)));
+  else
+    FGB_CUDA((fgb::launch_pack_f32<float>(n, m->pos[m->cur], m->vel[m->cur], F, m->d_io, m->stream)));
+  m->host_pts.resize(10 * size_t(n));
+  FGB_CUDA(cudaMemcpyAsync(m->host_pts.data(), m->d_io, 10 * sizeof(float) * size_t(n), cudaMemcpyDeviceToHost,
+                           m->stream));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  return FGB_OK;
+}
+
+int upload_pins(fgb_mesh* m) {
+  const uint32_t n = m->topo.n;
+  std::vector<uint8_t> pinned(n, 0);
+  for (uint32_t p : m->topo.pins) pinned[p] = 1;
+  FGB_CUDA(dalloc(m->d_pinned, n));
+  FGB_CUDA(cudaMemcpy(m->d_pinned, pinned.data(), n, cudaMemcpyHostToDevice));
+  m->pins_dirty = false;
+  return FGB_OK;
+}
+
+int alloc_state(fgb_mesh* m) {
+  const size_t bytes = m->elem() * size_t(m->topo.n);
+  for (int i = 0; i < 2; ++i) {
+    if (!m->pos[i]) FGB_CUDA(dalloc(m->pos[i], bytes));
+    if (!m->vel[i]) FGB_CUDA(dalloc(m->vel[i], bytes));
+  }
+  if (!m->d_flags) {
+    FGB_CUDA(dalloc(m->d_flags, sizeof(unsigned)));
+    FGB_CUDA(cudaMemsetAsync(m->d_flags, 0, sizeof(unsigned), m->stream));
+  }
+  return FGB_OK;
+}
+
+int ensure_force(fgb_mesh* m) {
+  if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * size_t(m->topo.n)));
+  if (!m->has_force) {
+    FGB_CUDA(cudaMemsetAsync(m->force, 0, m->elem() * size_t(m->topo.n), m->stream));
+    m->has_force = true;
+  }
+  return FGB_OK;
+}
+
+// host_pts -> device (pos/vel, and force when any accumulated force is set).
+int upload_state(fgb_mesh* m) {
+  const int n = int(m->topo.n);
+  FGB_CHECK_RC(alloc_state(m));
+  bool any_force = false;
+  for (int i = 0; i < n && !any_force; ++i) {
+    const float* p = &m->host_pts[10 * size_t(i)];
+    any_force = p[7] != 0.0f || p[8] != 0.0f || p[9] != 0.0f || std::signbit(p[7]) || std::signbit(p[8]) ||
+                std::signbit(p[9]);
+  }
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * size_t(n)));
+  FGB_CUDA(cudaMemcpyAsync(m->d_io, m->host_pts.data(), 10 * sizeof(float) * size_t(n), cudaMemcpyHostToDevice,
+                           m->stream));
+  void* F = nullptr;
+  if (any_force) {
+    if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * size_t(n)));
+    F = m->force;
+  }
+  m->cur = 0;
+  if (m->precision == 64)
+    FGB_CUDA((fgb::launch_unpack<double>(n, m->d_io, m->d_pinned, m->pos[0], m->vel[0], F, m->stream)));
+  else
+    FGB_CUDA((fgb::launch_unpack<float>(n, m->d_io, m->d_pinned, m->pos[0], m->vel[0], F, m->stream)));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  m->has_force = any_force;
+  m->staged = false;
+  m->state_on_device = true;
+  return FGB_OK;
+}
+
+int ensure_csr(fgb_mesh* m) {
+  if (m->csr_ready) return FGB_OK;
+  fgb::CsrTopo t;
+  std::string err;
+  FGB_CHECK_RC(fgb::build_csr(m->topo, t, err) ? fail(FGB_EINVAL, err) : FGB_OK);
+  FGB_CUDA(dalloc(m->d_strut_off, t.strut_off.size() * sizeof(int)));
+  FGB_CUDA(dalloc(m->d_strut_inc, t.strut_inc.size() * sizeof(int)));
+  FGB_CUDA(dalloc(m->d_strut_kcl, t.strut_kcl.size() * sizeof(float)));
+  FGB_CUDA(dalloc(m->d_face_off, t.face_off.size() * sizeof(int)));
+  FGB_CUDA(dalloc(m->d_face_inc, t.face_inc.size() * sizeof(int)));
+  FGB_CUDA(dalloc(m->d_face_vtx, t.face_vtx.size() * sizeof(int)));
+  FGB_CUDA(cudaMemcpy(m->d_strut_off, t.strut_off.data(), t.strut_off.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FGB_CUDA(cudaMemcpy(m->d_strut_inc, t.strut_inc.data(), t.strut_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FGB_CUDA(cudaMemcpy(m->d_strut_kcl, t.strut_kcl.data(), t.strut_kcl.size() * sizeof(float),
+                      cudaMemcpyHostToDevice));
+  FGB_CUDA(cudaMemcpy(m->d_face_off, t.face_off.data(), t.face_off.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FGB_CUDA(cudaMemcpy(m->d_face_inc, t.face_inc.data(), t.face_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
+  FGB_CUDA(cudaMemcpy(m->d_face_vtx, t.face_vtx.data(), t.face_vtx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  m->csr_ready = true;
+  return FGB_OK;
+}
+
+// Path choice (host only): 2 = grid kernel, 1 = general gather.
+int decide_path(fgb_mesh* m, int* path) {
+  const bool grid_ok = m->precision == 32 && m->topo.rows > 0 && fgb::grid_layout_ok(m->topo);
+  if (m->path_req == 2 && !grid_ok)
+    return fail(FGB_ESTATE, "grid path requested but the mesh is not a Cloth::new grid (or precision is f64)");
+  *path = (m->path_req == 1 || !grid_ok) ? 1 : 2;
+  return FGB_OK;
+}
+
+// Topology upload.
+int ensure_topology(fgb_mesh* m) {
+  if (!m->topo_dirty) return FGB_OK;
+  free_topology(m);
+  FGB_CHECK_RC(decide_path(m, &m->active_path));
+  if (m->active_path == 2) {
+    std::vector<float> planes;
+    fgb::build_grid_params(m->topo, planes);
+    FGB_CUDA(dalloc(m->d_grid, planes.size() * sizeof(float)));
+    FGB_CUDA(cudaMemcpy(m->d_grid, planes.data(), planes.size() * sizeof(float), cudaMemcpyHostToDevice));
+  } else {
+    FGB_CHECK_RC(ensure_csr(m));
+  }
+  m->topo_dirty = false;
+  return FGB_OK;
+}
+
+int ensure_device(fgb_mesh* m) {
+  FGB_CUDA(cudaSetDevice(m->device));
+  FGB_CHECK_RC(ensure_stream(m));
+  if (m->pins_dirty) {
+    if (m->state_on_device) {
+      FGB_CHECK_RC(download_state(m));
+      m->state_on_device = false;
+    }
+    FGB_CHECK_RC(upload_pins(m));
+  }
+  FGB_CHECK_RC(ensure_topology(m));
+  if (!m->state_on_device) FGB_CHECK_RC(upload_state(m));
+  return FGB_OK;
+}
+
+fgb::StepConsts make_consts(const fgb_config& cfg, const fgb::ObsFace* faces, int n_faces, unsigned* flags) {
+  fgb::StepConsts c;
+  c.integration = cfg.integration;
+  c.dt = cfg.dt;
+  c.dt_duration = fgb::duration_roundtrip(cfg.dt);
+  for (int i = 0; i < 3; ++i) {
+    c.force0[i] = 0.0f + cfg.gravity[i];
+    c.wind[i] = cfg.wind[i];
+  }
+  c.neg_drag = -1.0f * cfg.drag_coefficient;
+  c.neg_lift = -1.0f * cfg.lift_coefficient;
+  c.restitution = cfg.coefficient_of_restitution;
+  c.friction = cfg.coefficient_of_friction;
+  c.n_obstacle_faces = n_faces;
+  c.obstacle_faces = faces;
+  c.flags = flags;
+  return c;
+}
+
+int check_config(const fgb_config* cfg) {
+  if (!cfg) return fail(FGB_EINVAL, "null config");
+  if (cfg->integration != FGB_EULER && cfg->integration != FGB_RK4) return fail(FGB_EINVAL, "bad integration");
+  // Duration::from_secs_f32 panics on negative, NaN or overflowing input.
+  if (!finite_nonneg(cfg->dt) || cfg->dt > 1.0e9f) return fail(FGB_EINVAL, "dt must be finite, >= 0 and < 1e9 s");
+  return FGB_OK;
+}
+
+// One fused Simulation::step of one mesh.
+int step_mesh(fgb_mesh* m, const fgb::StepConsts& c) {
+  const int n = int(m->topo.n);
+  const int nxt = m->cur ^ 1;
+  const void* F = m->has_force ? m->force : nullptr;
+  if (m->active_path == 2) {
+    fgb::GridTopo g{int(m->topo.rows), int(m->topo.cols), m->d_grid};
+    FGB_CUDA(fgb::launch_step_grid(g, static_cast<const float4*>(m->pos[m->cur]),
+                                   static_cast<const float4*>(m->vel[m->cur]), static_cast<const float4*>(F),
+                                   static_cast<float4*>(m->pos[nxt]), static_cast<float4*>(m->vel[nxt]), c,
+                                   m->stream));
+  } else {
+    fgb::GeneralTopo t{m->d_strut_off, m->d_strut_inc, m->d_strut_kcl, m->d_face_off, m->d_face_inc, m->d_face_vtx};
+    if (m->precision == 64)
+      FGB_CUDA(fgb::launch_step_general<double>(n, m->pos[m->cur], m->vel[m->cur], F, m->pos[nxt], m->vel[nxt], t,
+                                                c, m->stream));
+    else
+      FGB_CUDA(fgb::launch_step_general<float>(n, m->pos[m->cur], m->vel[m->cur], F, m->pos[nxt], m->vel[nxt], t,
+                                               c, m->stream));
+  }
+  m->cur = nxt;
+  m->has_force = false;  // clear_forces
+  m->staged = false;
+  return FGB_OK;
+}
+
+int make_obstacle_faces(fgb_obstacle* const* obs, uint64_t nobs, std::vector<fgb::ObsFace>& out) {
+  out.clear();
+  for (uint64_t i = 0; i < nobs; ++i) {
+    if (!obs[i]) return fail(FGB_EINVAL, "null obstacle");
+    out.insert(out.end(), obs[i]->faces.begin(), obs[i]->faces.end());
+  }
+  if (out.size() > 0x7fffffffull) return fail(FGB_EINVAL, "too many obstacle faces");
+  return FGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fgb_last_error(void) { return g_err.c_str(); }
+
+int fgb_config_default(fgb_config* out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  std::memset(out, 0, sizeof(*out));
+  out->integration = FGB_RK4;
+  out->dt = fgb::duration_roundtrip(0.001f);  // Duration::from_millis(1).as_secs_f32()
+  out->gravity[1] = -10.0f;
+  out->lift_coefficient = 1.0f;
+  out->drag_coefficient = 1.0f;
+  out->coefficient_of_restitution = 0.95f;
+  out->coefficient_of_friction = 0.3f;
+  return FGB_OK;
+}
+
+static int finish_new_mesh(MeshTopo&& topo, fgb_mesh** out) {
+  fgb_mesh* m = new (std::nothrow) fgb_mesh();
+  if (!m) return fail(FGB_ENOMEM, "out of host memory");
+  m->topo = std::move(topo);
+  cudaGetDevice(&m->device);
+  init_host_state(m);
+  *out = m;
+  return FGB_OK;
+}
+
+int fgb_mesh_new(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                 float mass, float default_stiffness, float default_damping, const fgb_spring_override* overrides,
+                 uint64_t n_overrides, fgb_mesh** out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  *out = nullptr;
+  std::vector<fgb::Override> ov(n_overrides);
+  for (uint64_t i = 0; i < n_overrides; ++i)
+    ov[i] = fgb::Override{overrides[i].a, overrides[i].b, overrides[i].stiffness, overrides[i].damping};
+  MeshTopo topo;
+  std::string err;
+  try {
+    const int rc = fgb::build_springy(positions, n_vertices, indices, n_indices, mass, default_stiffness,
+                                      default_damping, ov.data(), n_overrides, topo, err);
+    if (rc) return fail(rc, err);
+  } catch (const std::bad_alloc&) {
+    return fail(FGB_ENOMEM, "out of host memory");
+  }
+  return finish_new_mesh(std::move(topo), out);
+}
+
+int fgb_cloth_new(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass,
+                  float tensile_stiffness, float tensile_damping, float shear_stiffness, float shear_damping,
+                  float binding_stiffness, float binding_damping, const uint32_t* pinned, uint64_t n_pinned,
+                  fgb_mesh** out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  *out = nullptr;
+  MeshTopo topo;
+  std::string err;
+  try {
+    const int rc = fgb::build_cloth(rows, cols, spacing, position, point_mass, tensile_stiffness, tensile_damping,
+                                    shear_stiffness, shear_damping, binding_stiffness, binding_damping, pinned,
+                                    n_pinned, topo, err);
+    if (rc) return fail(rc, err);
+  } catch (const std::bad_alloc&) {
+    return fail(FGB_ENOMEM, "out of host memory");
+  }
+  return finish_new_mesh(std::move(topo), out);
+}
+
+int fgb_mesh_add_strut(fgb_mesh* m, uint32_t a, uint32_t b, float stiffness, float damping) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  // The rest length uses the points' current positions (springy_mesh.rs:407-408).
+  FGB_CHECK_RC(download_state(m));
+  std::vector<float> cur(3 * size_t(m->topo.n));
+  for (uint32_t i = 0; i < m->topo.n; ++i)
+    for (int k = 0; k < 3; ++k) cur[3 * size_t(i) + k] = m->host_pts[10 * size_t(i) + 1 + k];
+  std::string err;
+  const int rc = fgb::add_strut(m->topo, a, b, stiffness, damping, cur.data(), err);
+  if (rc) return fail(rc, err);
+  m->state_on_device = false;  // host_pts is current; re-upload with the new topology
+  m->topo_dirty = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_add_pin(fgb_mesh* m, uint32_t index) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (index >= m->topo.n) return fail(FGB_EINDEX, "pin index out of range");
+  m->topo.pins.push_back(index);
+  m->pins_dirty = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_counts(const fgb_mesh* m, uint64_t out[4]) {
+  if (!m || !out) return fail(FGB_EINVAL, "null argument");
+  out[0] = m->topo.n;
+  out[1] = m->topo.sa.size();
+  out[2] = m->topo.fv.size() / 3;
+  out[3] = m->topo.pins.size();
+  return FGB_OK;
+}
+
+int fgb_mesh_get_struts(const fgb_mesh* m, float* kcl, uint32_t* ab) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  const size_t S = m->topo.sa.size();
+  for (size_t s = 0; s < S; ++s) {
+    if (kcl) {
+      kcl[3 * s] = m->topo.sk[s];
+      kcl[3 * s + 1] = m->topo.sc[s];
+      kcl[3 * s + 2] = m->topo.sl[s];
+    }
+    if (ab) {
+      ab[2 * s] = m->topo.sa[s];
+      ab[2 * s + 1] = m->topo.sb[s];
+    }
+  }
+  return FGB_OK;
+}
+
+int fgb_mesh_set_strut_params(fgb_mesh* m, const float* stiffness, const float* damping) {
+  if (!m || !stiffness || !damping) return fail(FGB_EINVAL, "null argument");
+  std::copy(stiffness, stiffness + m->topo.sk.size(), m->topo.sk.begin());
+  std::copy(damping, damping + m->topo.sc.size(), m->topo.sc.begin());
+  m->topo_dirty = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_get_points(fgb_mesh* m, float* out) {
+  if (!m || !out) return fail(FGB_EINVAL, "null argument");
+  const size_t n = m->topo.n;
+  if (!m->state_on_device) {
+    std::memcpy(out, m->host_pts.data(), 10 * sizeof(float) * n);
+    return FGB_OK;
+  }
+  FGB_CUDA(cudaSetDevice(m->device));
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
+  const void* F = m->has_force ? m->force : nullptr;
+  if (m->precision == 64)
+    FGB_CUDA((fgb::launch_pack_f32<double>(int(n), m->pos[m->cur], m->vel[m->cur], F, m->d_io, m->stream)));
+  else
+    FGB_CUDA((fgb::launch_pack_f32<float>(int(n), m->pos[m->cur], m->vel[m->cur], F, m->d_io, m->stream)));
+  FGB_CUDA(cudaMemcpyAsync(out, m->d_io, 10 * sizeof(float) * n, cudaMemcpyDeviceToHost, m->stream));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  return FGB_OK;
+}
+
+int fgb_mesh_get_points_f64(fgb_mesh* m, double* out) {
+  if (!m || !out) return fail(FGB_EINVAL, "null argument");
+  const size_t n = m->topo.n;
+  if (!m->state_on_device) {
+    for (size_t i = 0; i < 10 * n; ++i) out[i] = double(m->host_pts[i]);
+    return FGB_OK;
+  }
+  FGB_CUDA(cudaSetDevice(m->device));
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(double) * n));
+  const void* F = m->has_force ? m->force : nullptr;
+  double* d = reinterpret_cast<double*>(m->d_io);
+  if (m->precision == 64)
+    FGB_CUDA((fgb::launch_pack_f64<double>(int(n), m->pos[m->cur], m->vel[m->cur], F, d, m->stream)));
+  else
+    FGB_CUDA((fgb::launch_pack_f64<float>(int(n), m->pos[m->cur], m->vel[m->cur], F, d, m->stream)));
+  FGB_CUDA(cudaMemcpyAsync(out, d, 10 * sizeof(double) * n, cudaMemcpyDeviceToHost, m->stream));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  return FGB_OK;
+}
+
+int fgb_mesh_set_points(fgb_mesh* m, const float* in) {
+  if (!m || !in) return fail(FGB_EINVAL, "null argument");
+  const size_t n = m->topo.n;
+  if (!m->state_on_device || m->pins_dirty || m->topo_dirty) {
+    m->host_pts.assign(in, in + 10 * n);
+    m->state_on_device = false;
+    return FGB_OK;
+  }
+  // Device-resident: DMA the raw points and convert on the device.
+  FGB_CUDA(cudaSetDevice(m->device));
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
+  bool any_force = false;
+  for (size_t i = 0; i < n && !any_force; ++i)
+    any_force = in[10 * i + 7] != 0.0f || in[10 * i + 8] != 0.0f || in[10 * i + 9] != 0.0f ||
+                std::signbit(in[10 * i + 7]) || std::signbit(in[10 * i + 8]) || std::signbit(in[10 * i + 9]);
+  FGB_CUDA(cudaMemcpyAsync(m->d_io, in, 10 * sizeof(float) * n, cudaMemcpyHostToDevice, m->stream));
+  void* F = nullptr;
+  if (any_force) {
+    if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * n));
+    F = m->force;
+  }
+  if (m->precision == 64)
+    FGB_CUDA((fgb::launch_unpack<double>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], F, m->stream)));
+  else
+    FGB_CUDA((fgb::launch_unpack<float>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], F, m->stream)));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  m->has_force = any_force;
+  m->staged = false;
+  return FGB_OK;
+}
+
+int fgb_mesh_get_positions(fgb_mesh* m, float* out) {
+  if (!m || !out) return fail(FGB_EINVAL, "null argument");
+  const size_t n = m->topo.n;
+  if (!m->state_on_device) {
+    for (size_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) out[3 * i + k] = m->host_pts[10 * i + 1 + k];
+    return FGB_OK;
+  }
+  FGB_CUDA(cudaSetDevice(m->device));
+  FGB_CHECK_RC(ensure_io(m, 3 * sizeof(float) * n));
+  if (m->precision == 64)
+    FGB_CUDA(fgb::launch_positions<double>(int(n), m->pos[m->cur], m->d_io, m->stream));
+  else
+    FGB_CUDA(fgb::launch_positions<float>(int(n), m->pos[m->cur], m->d_io, m->stream));
+  FGB_CUDA(cudaMemcpyAsync(out, m->d_io, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, m->stream));
+  FGB_CUDA(cudaStreamSynchronize(m->stream));
+  return FGB_OK;
+}
+
+int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (positions) FGB_CHECK_RC(fgb_mesh_get_positions(m, positions));
+  if (indices) std::memcpy(indices, m->topo.fv.data(), m->topo.fv.size() * sizeof(uint32_t));
+  return FGB_OK;
+}
+
+int fgb_mesh_set_path(fgb_mesh* m, int path) {
+  if (!m || path < 0 || path > 2) return fail(FGB_EINVAL, "path must be 0, 1 or 2");
+  m->path_req = path;
+  m->topo_dirty = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_get_path(fgb_mesh* m, int* path) {
+  if (!m || !path) return fail(FGB_EINVAL, "null argument");
+  if (!m->topo_dirty) {
+    *path = m->active_path;
+    return FGB_OK;
+  }
+  return decide_path(m, path);
+}
+
+int fgb_mesh_set_precision(fgb_mesh* m, int bits) {
+  if (!m || (bits != 32 && bits != 64)) return fail(FGB_EINVAL, "precision must be 32 or 64");
+  if (bits == m->precision) return FGB_OK;
+  FGB_CHECK_RC(download_state(m));
+  m->state_on_device = false;
+  free_state(m);
+  m->precision = bits;
+  m->topo_dirty = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_accumulate_forces(fgb_mesh* m, const fgb_config* cfg) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  FGB_CHECK_RC(check_config(cfg));
+  FGB_CHECK_RC(ensure_device(m));
+  FGB_CHECK_RC(ensure_csr(m));
+  FGB_CHECK_RC(ensure_force(m));
+  const fgb::StepConsts c = make_consts(*cfg, nullptr, 0, m->d_flags);
+  fgb::GeneralTopo t{m->d_strut_off, m->d_strut_inc, m->d_strut_kcl, m->d_face_off, m->d_face_inc, m->d_face_vtx};
+  if (m->precision == 64)
+    FGB_CUDA(fgb::launch_accumulate<double>(int(m->topo.n), m->pos[m->cur], m->vel[m->cur], m->force, t, c, m->stream));
+  else
+    FGB_CUDA(fgb::launch_accumulate<float>(int(m->topo.n), m->pos[m->cur], m->vel[m->cur], m->force, t, c, m->stream));
+  return FGB_OK;
+}
+
+int fgb_mesh_integrate(fgb_mesh* m, int32_t integration, float dt) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (integration != FGB_EULER && integration != FGB_RK4) return fail(FGB_EINVAL, "bad integration");
+  FGB_CHECK_RC(ensure_device(m));
+  FGB_CHECK_RC(ensure_force(m));
+  const size_t bytes = m->elem() * size_t(m->topo.n);
+  if (!m->spos) FGB_CUDA(dalloc(m->spos, bytes));
+  if (!m->svel) FGB_CUDA(dalloc(m->svel, bytes));
+  if (!m->sforce) FGB_CUDA(dalloc(m->sforce, bytes));
+  if (m->precision == 64)
+    FGB_CUDA(fgb::launch_integrate<double>(int(m->topo.n), integration, dt, m->pos[m->cur], m->vel[m->cur], m->force,
+                                           m->spos, m->svel, m->sforce, m->stream));
+  else
+    FGB_CUDA(fgb::launch_integrate<float>(int(m->topo.n), integration, dt, m->pos[m->cur], m->vel[m->cur], m->force,
+                                          m->spos, m->svel, m->sforce, m->stream));
+  m->staged = true;
+  return FGB_OK;
+}
+
+int fgb_mesh_update_points(fgb_mesh* m, fgb_obstacle* const* obstacles, uint64_t n_obstacles, const fgb_config* cfg) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  FGB_CHECK_RC(check_config(cfg));
+  if (!m->staged) return fail(FGB_ESTATE, "update_points needs staged points: call fgb_mesh_integrate first");
+  if (n_obstacles && !obstacles) return fail(FGB_EINVAL, "null obstacle list");
+  std::vector<fgb::ObsFace> faces;
+  FGB_CHECK_RC(make_obstacle_faces(obstacles, n_obstacles, faces));
+  fgb::ObsFace* d_faces = nullptr;
+  FGB_CUDA(dalloc(d_faces, faces.size() * sizeof(fgb::ObsFace)));
+  FGB_CUDA(cudaMemcpy(d_faces, faces.data(), faces.size() * sizeof(fgb::ObsFace), cudaMemcpyHostToDevice));
+  const fgb::StepConsts c = make_consts(*cfg, d_faces, int(faces.size()), m->d_flags);
+  cudaError_t e;
+  if (m->precision == 64)
+    e = fgb::launch_update<double>(int(m->topo.n), m->pos[m->cur], m->vel[m->cur], m->force, m->spos, m->svel,
+                                   m->sforce, c, m->stream);
+  else
+    e = fgb::launch_update<float>(int(m->topo.n), m->pos[m->cur], m->vel[m->cur], m->force, m->spos, m->svel,
+                                  m->sforce, c, m->stream);
+  const cudaError_t s = cudaStreamSynchronize(m->stream);
+  dfree(d_faces);
+  FGB_CUDA(e);
+  FGB_CUDA(s);
+  m->staged = false;
+  return FGB_OK;
+}
+
+int fgb_mesh_clear_forces(fgb_mesh* m) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (!m->state_on_device) {
+    for (size_t i = 0; i < m->topo.n; ++i)
+      for (int k = 7; k < 10; ++k) m->host_pts[10 * i + k] = 0.0f;
+    return FGB_OK;
+  }
+  m->has_force = false;  // a missing force buffer reads as zero
+  return FGB_OK;
+}
+
+int fgb_mesh_synchronize(fgb_mesh* m) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
+  return FGB_OK;
+}
+
+int fgb_mesh_destroy(fgb_mesh* m) {
+  if (!m) return FGB_OK;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  free_state(m);
+  free_topology(m);
+  dfree(m->d_io);
+  dfree(m->d_pinned);
+  dfree(m->d_flags);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+  return FGB_OK;
+}
+
+int fgb_collidable_new(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                       fgb_obstacle** out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  *out = nullptr;
+  if ((n_vertices && !positions) || (n_indices && !indices)) return fail(FGB_EINVAL, "null buffer");
+  const uint64_t nt = n_indices / 3;
+  std::set<std::pair<uint32_t, uint32_t>> edges;
+  std::vector<fgb::ObsFace> faces;
+  faces.reserve(nt);
+  for (uint64_t t = 0; t < nt; ++t) {
+    const uint32_t i[3] = {indices[3 * t], indices[3 * t + 1], indices[3 * t + 2]};
+    for (int k = 0; k < 3; ++k)
+      if (i[k] >= n_vertices) return fail(FGB_EINDEX, "collidable mesh index out of range");
+    if (i[0] == i[1] || i[1] == i[2] || i[2] == i[0])
+      return fail(FGB_EINVAL, "collidable mesh triangle repeats a vertex");
+    for (int k = 0; k < 3; ++k) edges.insert({std::min(i[k], i[(k + 1) % 3]), std::max(i[k], i[(k + 1) % 3])});
+    const float* p0 = positions + 3 * size_t(i[0]);
+    const float* p1 = positions + 3 * size_t(i[1]);
+    const float* p2 = positions + 3 * size_t(i[2]);
+    // Face::normal, collidable_mesh.rs:41-43: (v1 - v0).cross(v2 - v0).normalize()
+    const float ax = p1[0] - p0[0], ay = p1[1] - p0[1], az = p1[2] - p0[2];
+    const float bx = p2[0] - p0[0], by = p2[1] - p0[1], bz = p2[2] - p0[2];
+    const float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+    const float inv = 1.0f / std::sqrt(cx * cx + cy * cy + cz * cz);
+    const float nx = cx * inv, ny = cy * inv, nz = cz * inv;
+    // projection axis of collidable_mesh.rs:133-154 (signed comparisons)
+    int axis = 2;
+    if (nx >= ny && nx >= nz) axis = 0;
+    else if (ny >= nx && ny >= nz) axis = 1;
+    fgb::ObsFace f;
+    float axis_bits;
+    std::memcpy(&axis_bits, &axis, 4);
+    f.v0 = make_float4(p0[0], p0[1], p0[2], axis_bits);
+    f.v1 = make_float4(p1[0], p1[1], p1[2], 0.0f);
+    f.v2 = make_float4(p2[0], p2[1], p2[2], 0.0f);
+    f.n = make_float4(nx, ny, nz, 0.0f);
+    faces.push_back(f);
+  }
+  fgb_obstacle* o = new (std::nothrow) fgb_obstacle();
+  if (!o) return fail(FGB_ENOMEM, "out of host memory");
+  o->n_vertices = n_vertices;
+  o->n_edges = edges.size();
+  o->faces = std::move(faces);
+  *out = o;
+  return FGB_OK;
+}
+
+int fgb_collidable_counts(const fgb_obstacle* o, uint64_t out[3]) {
+  if (!o || !out) return fail(FGB_EINVAL, "null argument");
+  out[0] = o->n_vertices;
+  out[1] = o->n_edges;
+  out[2] = o->faces.size();
+  return FGB_OK;
+}
+
+int fgb_collidable_destroy(fgb_obstacle* o) {
+  delete o;
+  return FGB_OK;
+}
+
+int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
+                fgb_sim** out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  *out = nullptr;
+  if ((n_meshes && !meshes) || (n_obstacles && !obstacles)) return fail(FGB_EINVAL, "null list");
+  std::vector<fgb::ObsFace> faces;
+  FGB_CHECK_RC(make_obstacle_faces(obstacles, n_obstacles, faces));
+  for (uint64_t i = 0; i < n_meshes; ++i)
+    if (!meshes[i]) return fail(FGB_EINVAL, "null mesh");
+  fgb_sim* s = new (std::nothrow) fgb_sim();
+  if (!s) return fail(FGB_ENOMEM, "out of host memory");
+  s->meshes.assign(meshes, meshes + n_meshes);
+  s->obstacles.assign(obstacles, obstacles + n_obstacles);
+  fgb_config_default(&s->cfg);
+  s->n_faces = int(faces.size());
+  if (!faces.empty()) {
+    cudaError_t e = dalloc(s->d_faces, faces.size() * sizeof(fgb::ObsFace));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(s->d_faces, faces.data(), faces.size() * sizeof(fgb::ObsFace), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      dfree(s->d_faces);
+      delete s;
+      return fail(FGB_ECUDA, std::string("obstacle upload: ") + cudaGetErrorString(e));
+    }
+  }
+  *out = s;
+  return FGB_OK;
+}
+
+int fgb_sim_set_config(fgb_sim* s, const fgb_config* cfg) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  FGB_CHECK_RC(check_config(cfg));
+  s->cfg = *cfg;
+  return FGB_OK;
+}
+
+int fgb_sim_get_config(const fgb_sim* s, fgb_config* out) {
+  if (!s || !out) return fail(FGB_EINVAL, "null argument");
+  *out = s->cfg;
+  return FGB_OK;
+}
+
+int fgb_sim_step(fgb_sim* s, uint64_t n_steps) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_device(m));
+  for (uint64_t k = 0; k < n_steps; ++k)
+    for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags)));
+  return FGB_OK;
+}
+
+int fgb_sim_get_timestep(const fgb_sim* s, double* seconds) {
+  if (!s || !seconds) return fail(FGB_EINVAL, "null argument");
+  *seconds = fgb::duration_seconds_f64(s->cfg.dt);
+  return FGB_OK;
+}
+
+int fgb_sim_synchronize(fgb_sim* s, int* nonfinite) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  int bad = 0;
+  for (fgb_mesh* m : s->meshes) {
+    if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
+    if (m->d_flags) {
+      unsigned f = 0;
+      FGB_CUDA(cudaMemcpy(&f, m->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+      if (f) {
+        bad = 1;
+        FGB_CUDA(cudaMemsetAsync(m->d_flags, 0, sizeof(unsigned), m->stream));
+        FGB_CUDA(cudaStreamSynchronize(m->stream));
+      }
+    }
+  }
+  if (nonfinite) *nonfinite = bad;
+  return FGB_OK;
+}
+
+int fgb_sim_destroy(fgb_sim* s) {
+  if (!s) return FGB_OK;
+  for (fgb_mesh* m : s->meshes)
+    if (m->stream) cudaStreamSynchronize(m->stream);
+  dfree(s->d_faces);
+  delete s;
+  return FGB_OK;
+}
+
+}  // extern "C"

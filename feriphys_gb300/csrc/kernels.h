@@ -1,0 +1,47 @@
+// Host-visible launch wrappers of the device kernels (no CUDA types beyond
+// cudaStream_t/cudaError_t in the signatures).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "step_consts.h"
+
+namespace fgb {
+
+// CSR incidence lists of the general gather (see step_general.cu).
+struct GeneralTopo {
+  const int* strut_off;
+  const int2* strut_inc;
+  const float4* strut_kcl;
+  const int* face_off;
+  const int* face_inc;
+  const int4* face_vtx;
+};
+
+// Grid (Cloth::new topology) description for the stencil kernel (see
+// step_grid.cu).  params holds 4 planes of n float4 (owned-strut constants).
+struct GridTopo {
+  int rows, cols;
+  const float4* params;
+};
+
+template <class T>
+cudaError_t launch_step_general(int n, const void* pos, const void* vel, const void* force_in, void* pos_out,
+                                void* vel_out, const GeneralTopo& t, const StepConsts& c, cudaStream_t s);
+template <class T>
+cudaError_t launch_accumulate(int n, const void* pos, const void* vel, void* force, const GeneralTopo& t,
+                              const StepConsts& c, cudaStream_t s);
+template <class T>
+cudaError_t launch_integrate(int n, int integration, float h, const void* pos, const void* vel, const void* force,
+                             void* spos, void* svel, void* sforce, cudaStream_t s);
+template <class T>
+cudaError_t launch_update(int n, void* pos, void* vel, void* force, const void* spos, const void* svel,
+                          const void* sforce, const StepConsts& c, cudaStream_t s);
+template <class T>
+cudaError_t launch_zero4(int n, void* a, cudaStream_t s);
+
+cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4* vel, const float4* force_in,
+                             float4* pos_out, float4* vel_out, const StepConsts& c, cudaStream_t s);
+
+}  // namespace fgb

@@ -1,0 +1,74 @@
+// Host-side mesh construction with the reference's semantics and ordering
+// (SpringyMesh::new springy_mesh.rs:267-401, add_strut 403-413, add_pin
+// 415-417, Cloth::new cloth.rs:20-113), plus the device-layout builders:
+// CSR incidence lists for the general gather and the owned-strut parameter
+// planes for the grid stencil kernel.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "grid_order.h"
+
+namespace fgb {
+
+struct MeshTopo {
+  uint32_t n = 0;
+  std::vector<float> pos;  // 3n, positions used for rest lengths (construction time)
+  float mass_per_vert = 0.0f;
+  // struts in reference order
+  std::vector<uint32_t> sa, sb;
+  std::vector<float> sk, sc, sl;
+  // faces in reference order
+  std::vector<uint32_t> fv;  // 3 per face
+  std::vector<uint32_t> fs;  // 3 per face (strut ids)
+  std::vector<uint32_t> pins;
+  // set when the triangle list is exactly Cloth::new's for rows x cols
+  uint32_t rows = 0, cols = 0;
+  size_t tri_struts = 0;  // struts created from the triangle list
+};
+
+struct Override {
+  uint32_t a, b;
+  float k, c;
+};
+
+// Returns 0 or a negative fgb_status; err gets a message.
+int build_springy(const float* pos, uint64_t nv, const uint32_t* idx, uint64_t ni, float mass, float k, float c,
+                  const Override* ov, uint64_t nov, MeshTopo& out, std::string& err);
+int build_cloth(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass, float tk,
+                float tc, float sk, float sc, float bk, float bc, const uint32_t* pins, uint64_t npins,
+                MeshTopo& out, std::string& err);
+// add_strut: rest length from `cur_pos` (3n floats, the points' current positions).
+int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, std::string& err);
+
+// Strut::new's length scaling: NOMINAL_STRUT_LENGTH / length * nominal (springy_mesh.rs:83-84).
+inline float scaled(float nominal, float length) { return 1.0f / length * nominal; }
+
+// Duration::from_secs_f32(x).as_secs_f32() with modern Rust's rounding to
+// whole nanoseconds (nearest, ties to even).  x finite and >= 0.
+float duration_roundtrip(float x);
+// Duration::from_secs_f32(x).as_secs_f64().
+double duration_seconds_f64(float x);
+
+// CSR incidence lists for the general gather (see step_general.cu).
+struct CsrTopo {
+  std::vector<int> strut_off;       // n+1
+  std::vector<int> strut_inc;       // 2 per entry: other, strut<<1|role
+  std::vector<float> strut_kcl;     // 4 per strut
+  std::vector<int> face_off;        // n+1
+  std::vector<int> face_inc;        // face<<2|corner
+  std::vector<int> face_vtx;        // 4 per face
+};
+int build_csr(const MeshTopo& m, CsrTopo& out, std::string& err);
+
+// Grid detection: true when the mesh is Cloth::new's rows x cols grid with
+// exactly its binding struts after the triangle struts, and the strut ids
+// around every vertex ascend in the order the grid kernel sums them.
+bool grid_layout_ok(const MeshTopo& m);
+// Owned-strut constants, 4 float4 planes of n entries (see grid_order.h).
+void build_grid_params(const MeshTopo& m, std::vector<float>& planes /*16*n*/);
+
+}  // namespace fgb

@@ -1,0 +1,199 @@
+/*
+ * feriphys_gb300 -- GB300-native (sm_103a) spring-mass-damper cloth step.
+ *
+ * C ABI of the drop-in for feriphys's springy-mesh simulation path.  Every
+ * entry point mirrors one item of the reference's Rust API (cited as
+ * file:line relative to the reference project root); the reference has no FFI
+ * of its own, so these are the calls its Rust host would bind (see
+ * INTEGRATION.md for the extern "C" block and build.rs).
+ *
+ * Conventions
+ *  - Every function returns 0 (FGB_OK) on success or a negative fgb_status;
+ *    fgb_last_error() gives a message for the calling thread.  The reference
+ *    panics where these return an error.
+ *  - Handles own their device memory and CUDA stream.  A handle is not
+ *    thread-safe: drive it from one host thread at a time.
+ *  - Host buffers are caller-owned and copied in/out; vertex indices are
+ *    uint32 (the reference uses usize; meshes stay below 2^31 vertices).
+ *  - Points use the reference's Stateful layout (springy_mesh.rs:242-255):
+ *    10 floats per point [mass, px, py, pz, vx, vy, vz, Fx, Fy, Fz].
+ *  - Arithmetic is f32 like the reference (cgmath Vector3<f32>); a mesh can
+ *    be switched to f64 for the FP64 rerun used to state rounding error.
+ */
+#ifndef FERIPHYS_GB300_H
+#define FERIPHYS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fgb_status {
+  FGB_OK = 0,
+  FGB_EINVAL = -1,       /* bad argument (null pointer, bad size, bad dt)  */
+  FGB_EINDEX = -2,       /* vertex index out of range                       */
+  FGB_ENONMANIFOLD = -3, /* an edge has more than two faces (springy_mesh.rs:339) */
+  FGB_ECUDA = -4,        /* CUDA runtime error (message has the CUDA text)  */
+  FGB_ESTATE = -5,       /* call not valid in the handle's current state   */
+  FGB_ENOMEM = -6,       /* host or device allocation failed               */
+  FGB_ECHECK = -7        /* a device-side check failed (see message)       */
+} fgb_status;
+
+/* state.rs:4-8 */
+typedef enum fgb_integration { FGB_EULER = 0, FGB_RK4 = 1 } fgb_integration;
+
+/* springy/config.rs:9-18.  gravity is a FORCE added to every point
+ * (springy_mesh.rs:194-196); drag/lift have no air density
+ * (springy_mesh.rs:636-646). */
+typedef struct fgb_config {
+  int32_t integration; /* fgb_integration */
+  float dt;            /* seconds */
+  float gravity[3];
+  float wind[3];
+  float lift_coefficient;
+  float drag_coefficient;
+  float coefficient_of_restitution;
+  float coefficient_of_friction;
+} fgb_config;
+
+/* StrutKey + SpringConfig (springy_mesh.rs:38-42, 96-107): per-edge override
+ * of the default stiffness/damping used by SpringyMesh::new. */
+typedef struct fgb_spring_override {
+  uint32_t a, b;
+  float stiffness, damping;
+} fgb_spring_override;
+
+typedef struct fgb_mesh fgb_mesh;
+typedef struct fgb_obstacle fgb_obstacle;
+typedef struct fgb_sim fgb_sim;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* fgb_last_error(void);
+
+/* Config::default() -- springy/config.rs:20-32 (Rk4, dt = 1 ms, g = (0,-10,0),
+ * Cl = Cd = 1, e = 0.95, mu = 0.3). */
+int fgb_config_default(fgb_config* out);
+
+/* ---------------------------------------------------------------- meshes -- */
+
+/* SpringyMesh::new -- springy_mesh.rs:267-401.  positions: 3*n_vertices
+ * floats; indices: triangles (3 per face, trailing remainder ignored like
+ * itertools::tuples); mass: TOTAL mass (split evenly, line 277); overrides
+ * may be NULL.  Struts are de-duplicated in triangle order; stiffness and
+ * damping are scaled by 1/rest_length (lines 83-84).  Torsional springs are
+ * not built (the reference's force for them is disabled, lines 518-519). */
+int fgb_mesh_new(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                 float mass, float default_stiffness, float default_damping,
+                 const fgb_spring_override* overrides, uint64_t n_overrides, fgb_mesh** out);
+
+/* Cloth::new -- springy/cloth.rs:20-113 (rows, cols >= 2).  Builds the grid,
+ * its triangles, the shear overrides, the pins and the binding struts. */
+int fgb_cloth_new(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass,
+                  float tensile_stiffness, float tensile_damping, float shear_stiffness, float shear_damping,
+                  float binding_stiffness, float binding_damping, const uint32_t* pinned, uint64_t n_pinned,
+                  fgb_mesh** out);
+
+/* SpringyMesh::add_strut -- springy_mesh.rs:403-413 (vertex order kept). */
+int fgb_mesh_add_strut(fgb_mesh* m, uint32_t a, uint32_t b, float stiffness, float damping);
+
+/* SpringyMesh::add_pin -- springy_mesh.rs:415-417. */
+int fgb_mesh_add_pin(fgb_mesh* m, uint32_t index);
+
+/* Counts: out[0] points, out[1] struts, out[2] faces, out[3] pins. */
+int fgb_mesh_counts(const fgb_mesh* m, uint64_t out[4]);
+
+/* Per-strut stiffness/damping/rest length and vertex pair, in strut order
+ * (the reference keeps these private; exposed for parity checks).  Any
+ * pointer may be NULL. */
+int fgb_mesh_get_struts(const fgb_mesh* m, float* kcl /*3*S*/, uint32_t* ab /*2*S*/);
+
+/* Replace per-strut stiffness and damping (already length-scaled, strut
+ * order).  Extension with no reference counterpart: lets a caller build
+ * per-strut random stiffness without an override map. */
+int fgb_mesh_set_strut_params(fgb_mesh* m, const float* stiffness, const float* damping);
+
+/* SpringyMesh::get_points -- springy_mesh.rs:419-421, in the Stateful layout
+ * (10 floats per point). */
+int fgb_mesh_get_points(fgb_mesh* m, float* out);
+
+/* Stateful::from_state_vector for every point -- springy_mesh.rs:204-221. */
+int fgb_mesh_set_points(fgb_mesh* m, const float* in);
+
+/* Positions only (3 floats per point), and the same in f64 for an f64 mesh. */
+int fgb_mesh_get_positions(fgb_mesh* m, float* out);
+int fgb_mesh_get_points_f64(fgb_mesh* m, double* out);
+
+/* SpringyMesh::get_vertices -- springy_mesh.rs:500-513 (positions 3*N,
+ * indices 3*F; either pointer may be NULL). */
+int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices);
+
+/* Select the step implementation: 0 = automatic (grid kernel when the mesh
+ * is a Cloth::new grid, else the general gather), 1 = general gather,
+ * 2 = grid kernel (fails with FGB_ESTATE if the mesh is not a grid). */
+int fgb_mesh_set_path(fgb_mesh* m, int path);
+
+/* Which path the next step uses (1 general, 2 grid); decided on the host. */
+int fgb_mesh_get_path(fgb_mesh* m, int* path);
+
+/* Arithmetic precision of the device state: 32 (default) or 64 (FP64
+ * rerun of the same step on the GPU; general gather path only). */
+int fgb_mesh_set_precision(fgb_mesh* m, int bits);
+
+/* Phase hooks used by Simulation::step (springy/simulation.rs:27-45):
+ * accumulate_forces (springy_mesh.rs:515-525), State::euler_step/rk4_step
+ * into the mesh's staging points (state.rs:75-106), update_points with the
+ * staged points (springy_mesh.rs:423-497) and clear_forces (656-660).
+ * fgb_sim_step runs the fused equivalent in one launch. */
+int fgb_mesh_accumulate_forces(fgb_mesh* m, const fgb_config* cfg);
+int fgb_mesh_integrate(fgb_mesh* m, int32_t integration, float dt);
+int fgb_mesh_update_points(fgb_mesh* m, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
+                           const fgb_config* cfg);
+int fgb_mesh_clear_forces(fgb_mesh* m);
+
+/* Wait for the mesh's stream. */
+int fgb_mesh_synchronize(fgb_mesh* m);
+
+int fgb_mesh_destroy(fgb_mesh* m);
+
+/* -------------------------------------------------------------- obstacles -- */
+
+/* CollidableMesh::new -- collidable_mesh.rs:57-97 (triangle soup; a triangle
+ * that repeats a vertex is rejected like the reference's panic at 81-89). */
+int fgb_collidable_new(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                       fgb_obstacle** out);
+/* Counts: out[0] vertices, out[1] edges, out[2] faces. */
+int fgb_collidable_counts(const fgb_obstacle* o, uint64_t out[3]);
+int fgb_collidable_destroy(fgb_obstacle* o);
+
+/* ------------------------------------------------------------- simulation -- */
+
+/* Simulation::new -- springy/simulation.rs:17-25 (starts from
+ * Config::default()).  The simulation borrows the meshes and obstacles:
+ * destroy it before them. */
+int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
+                fgb_sim** out);
+
+/* sync_sim_config_from_ui -- springy/simulation.rs:64-77 (headless form). */
+int fgb_sim_set_config(fgb_sim* s, const fgb_config* cfg);
+int fgb_sim_get_config(const fgb_sim* s, fgb_config* out);
+
+/* Simulation::step repeated n_steps times -- springy/simulation.rs:27-45.
+ * Asynchronous: returns once the launches are queued. */
+int fgb_sim_step(fgb_sim* s, uint64_t n_steps);
+
+/* Simulation::get_timestep -- springy/simulation.rs:47-49, as
+ * Duration::from_secs_f32(dt).as_secs_f64(). */
+int fgb_sim_get_timestep(const fgb_sim* s, double* seconds);
+
+/* Wait for every queued step; then report whether any stepped vertex went
+ * non-finite since the last call (*nonfinite = 1).  May be NULL. */
+int fgb_sim_synchronize(fgb_sim* s, int* nonfinite);
+
+int fgb_sim_destroy(fgb_sim* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FERIPHYS_GB300_H */
