@@ -102,6 +102,8 @@ def _declare(l):
         "fgb_cloth_new": (I, [U64, U64, F, P, F, F, F, F, F, F, F, P, U64, pp]),
         "fgb_mesh_add_strut": (I, [P, U32, U32, F, F]),
         "fgb_mesh_add_pin": (I, [P, U32]),
+        "fgb_mesh_add_struts": (I, [P, P, P, P, P, U64]),
+        "fgb_mesh_add_pins": (I, [P, P, U64]),
         "fgb_mesh_counts": (I, [P, P]),
         "fgb_mesh_get_struts": (I, [P, P, P]),
         "fgb_mesh_set_strut_params": (I, [P, P, P]),
@@ -126,6 +128,7 @@ def _declare(l):
         "fgb_sim_set_config": (I, [P, cfg]),
         "fgb_sim_get_config": (I, [P, cfg]),
         "fgb_sim_step": (I, [P, U64]),
+        "fgb_sim_set_stream": (I, [P, P]),
         "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
         "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
         "fgb_sim_destroy": (I, [P]),
@@ -217,6 +220,20 @@ class SpringyMesh:
 
     def add_pin(self, pin_index):
         _check(_lib().fgb_mesh_add_pin(self._h, int(pin_index)))
+
+    def add_struts(self, pairs, stiffness, damping):
+        """add_strut for each row of pairs [n, 2], in order."""
+        pairs = np.asarray(pairs, np.uint32).reshape(-1, 2)
+        n = len(pairs)
+        a = np.ascontiguousarray(pairs[:, 0])
+        b = np.ascontiguousarray(pairs[:, 1])
+        k = np.ascontiguousarray(np.broadcast_to(np.asarray(stiffness, np.float32), (n,)))
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(damping, np.float32), (n,)))
+        _check(_lib().fgb_mesh_add_struts(self._h, _ptr(a), _ptr(b), _ptr(k), _ptr(c), n))
+
+    def add_pins(self, pins):
+        p = _u32(pins)
+        _check(_lib().fgb_mesh_add_pins(self._h, _ptr(p), p.size))
 
     def counts(self):
         out = np.zeros(4, np.uint64)
@@ -393,6 +410,11 @@ class Simulation:
         simulated seconds of one step like the reference's Duration."""
         _check(_lib().fgb_sim_step(self._h, int(n_steps)))
         return self.get_timestep()
+
+    def set_stream(self, stream_handle):
+        """Issue every mesh's work on an external cudaStream_t (an integer
+        handle, e.g. torch.cuda.current_stream().cuda_stream); None resets."""
+        _check(_lib().fgb_sim_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
 
     def get_timestep(self) -> float:
         s = C.c_double()

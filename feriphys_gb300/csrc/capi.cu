@@ -71,7 +71,9 @@ struct fgb_mesh {
   int path_req = 0;      // 0 auto, 1 general, 2 grid
   int precision = 32;    // 32 or 64
   int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // the stream all work of this mesh is issued on
+  cudaStream_t own_stream = nullptr;  // created by the library (destroyed with the mesh)
+  bool external_stream = false;
 
   // host copy of the state while the device does not hold it (as_state layout)
   std::vector<float> host_pts;
@@ -112,8 +114,10 @@ struct fgb_sim {
   std::vector<fgb_mesh*> meshes;
   std::vector<fgb_obstacle*> obstacles;
   fgb_config cfg;
+  std::vector<fgb::ObsFace> faces;  // flattened obstacle faces (uploaded at the first step)
   fgb::ObsFace* d_faces = nullptr;
   int n_faces = 0;
+  bool faces_uploaded = false;
 };
 
 namespace {
@@ -132,7 +136,8 @@ void init_host_state(fgb_mesh* m) {
 }
 
 int ensure_stream(fgb_mesh* m) {
-  if (!m->stream) FGB_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  if (!m->own_stream) FGB_CUDA(cudaStreamCreateWithFlags(&m->own_stream, cudaStreamNonBlocking));
+  if (!m->external_stream) m->stream = m->own_stream;
   return FGB_OK;
 }
 
@@ -442,24 +447,37 @@ int fgb_cloth_new(uint64_t rows, uint64_t cols, float spacing, const float posit
 }
 
 int fgb_mesh_add_strut(fgb_mesh* m, uint32_t a, uint32_t b, float stiffness, float damping) {
+  return fgb_mesh_add_struts(m, &a, &b, &stiffness, &damping, 1);
+}
+
+int fgb_mesh_add_struts(fgb_mesh* m, const uint32_t* a, const uint32_t* b, const float* stiffness,
+                        const float* damping, uint64_t n) {
   if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (n && (!a || !b || !stiffness || !damping)) return fail(FGB_EINVAL, "null buffer");
   // The rest length uses the points' current positions (springy_mesh.rs:407-408).
   FGB_CHECK_RC(download_state(m));
-  std::vector<float> cur(3 * size_t(m->topo.n));
-  for (uint32_t i = 0; i < m->topo.n; ++i)
-    for (int k = 0; k < 3; ++k) cur[3 * size_t(i) + k] = m->host_pts[10 * size_t(i) + 1 + k];
   std::string err;
-  const int rc = fgb::add_strut(m->topo, a, b, stiffness, damping, cur.data(), err);
-  if (rc) return fail(rc, err);
+  for (uint64_t i = 0; i < n; ++i) {
+    const int rc = fgb::add_strut(m->topo, a[i], b[i], stiffness[i], damping[i], m->host_pts.data() + 1, 10, err);
+    if (rc) {
+      m->state_on_device = false;
+      m->topo_dirty = true;
+      return fail(rc, err);
+    }
+  }
   m->state_on_device = false;  // host_pts is current; re-upload with the new topology
   m->topo_dirty = true;
   return FGB_OK;
 }
 
-int fgb_mesh_add_pin(fgb_mesh* m, uint32_t index) {
+int fgb_mesh_add_pin(fgb_mesh* m, uint32_t index) { return fgb_mesh_add_pins(m, &index, 1); }
+
+int fgb_mesh_add_pins(fgb_mesh* m, const uint32_t* index, uint64_t n) {
   if (!m) return fail(FGB_EINVAL, "null mesh");
-  if (index >= m->topo.n) return fail(FGB_EINDEX, "pin index out of range");
-  m->topo.pins.push_back(index);
+  if (n && !index) return fail(FGB_EINVAL, "null buffer");
+  for (uint64_t i = 0; i < n; ++i)
+    if (index[i] >= m->topo.n) return fail(FGB_EINDEX, "pin index out of range");
+  m->topo.pins.insert(m->topo.pins.end(), index, index + n);
   m->pins_dirty = true;
   return FGB_OK;
 }
@@ -707,7 +725,7 @@ int fgb_mesh_destroy(fgb_mesh* m) {
   dfree(m->d_io);
   dfree(m->d_pinned);
   dfree(m->d_flags);
-  if (m->stream) cudaStreamDestroy(m->stream);
+  if (m->own_stream) cudaStreamDestroy(m->own_stream);
   delete m;
   return FGB_OK;
 }
@@ -787,16 +805,7 @@ int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const*
   s->obstacles.assign(obstacles, obstacles + n_obstacles);
   fgb_config_default(&s->cfg);
   s->n_faces = int(faces.size());
-  if (!faces.empty()) {
-    cudaError_t e = dalloc(s->d_faces, faces.size() * sizeof(fgb::ObsFace));
-    if (e == cudaSuccess)
-      e = cudaMemcpy(s->d_faces, faces.data(), faces.size() * sizeof(fgb::ObsFace), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      dfree(s->d_faces);
-      delete s;
-      return fail(FGB_ECUDA, std::string("obstacle upload: ") + cudaGetErrorString(e));
-    }
-  }
+  s->faces = std::move(faces);
   *out = s;
   return FGB_OK;
 }
@@ -816,9 +825,27 @@ int fgb_sim_get_config(const fgb_sim* s, fgb_config* out) {
 
 int fgb_sim_step(fgb_sim* s, uint64_t n_steps) {
   if (!s) return fail(FGB_EINVAL, "null sim");
+  if (!s->faces_uploaded) {
+    if (!s->faces.empty()) {
+      FGB_CUDA(dalloc(s->d_faces, s->faces.size() * sizeof(fgb::ObsFace)));
+      FGB_CUDA(cudaMemcpy(s->d_faces, s->faces.data(), s->faces.size() * sizeof(fgb::ObsFace),
+                          cudaMemcpyHostToDevice));
+    }
+    s->faces_uploaded = true;
+  }
   for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_device(m));
   for (uint64_t k = 0; k < n_steps; ++k)
     for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags)));
+  return FGB_OK;
+}
+
+int fgb_sim_set_stream(fgb_sim* s, void* stream) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  for (fgb_mesh* m : s->meshes) {
+    if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
+    m->external_stream = stream != nullptr;
+    m->stream = stream ? static_cast<cudaStream_t>(stream) : m->own_stream;
+  }
   return FGB_OK;
 }
 

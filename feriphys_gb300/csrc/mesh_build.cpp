@@ -67,11 +67,13 @@ class PairMap {
   size_t mask_;
 };
 
-inline float length_between(const float* pos, uint32_t a, uint32_t b) {
+inline float length_between(const float* pos, uint32_t a, uint32_t b, size_t stride = 3) {
   // (points[a].position - points[b].position).magnitude()
-  const float dx = pos[3 * a] - pos[3 * b];
-  const float dy = pos[3 * a + 1] - pos[3 * b + 1];
-  const float dz = pos[3 * a + 2] - pos[3 * b + 2];
+  const float* pa = pos + stride * a;
+  const float* pb = pos + stride * b;
+  const float dx = pa[0] - pb[0];
+  const float dy = pa[1] - pb[1];
+  const float dz = pa[2] - pb[2];
   return std::sqrt(dx * dx + dy * dy + dz * dz);
 }
 
@@ -230,12 +232,13 @@ int build_springy(const float* pos, uint64_t nv, const uint32_t* idx, uint64_t n
   return FGB_OK;
 }
 
-int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, std::string& err) {
+int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, size_t stride,
+              std::string& err) {
   if (a >= m.n || b >= m.n) {
     err = "strut vertex out of range";
     return FGB_EINDEX;
   }
-  const float L = length_between(cur_pos, a, b);
+  const float L = length_between(cur_pos, a, b, stride);
   m.sa.push_back(a);
   m.sb.push_back(b);
   m.sk.push_back(scaled(k, L));
@@ -301,8 +304,8 @@ int build_cloth(uint64_t rows, uint64_t cols, float spacing, const float positio
   for (uint64_t r = 0; r + 2 < rows; ++r)
     for (uint64_t c = 0; c + 2 < cols; ++c) {
       const uint32_t i = uint32_t(r * cols + c);
-      add_strut(m, i, i + 2, bk, bc, pos.data(), err);
-      add_strut(m, i, i + 2 * uint32_t(cols), bk, bc, pos.data(), err);
+      add_strut(m, i, i + 2, bk, bc, pos.data(), 3, err);
+      add_strut(m, i, i + 2 * uint32_t(cols), bk, bc, pos.data(), 3, err);
     }
   return FGB_OK;
 }

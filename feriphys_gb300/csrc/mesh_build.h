@@ -41,8 +41,10 @@ int build_springy(const float* pos, uint64_t nv, const uint32_t* idx, uint64_t n
 int build_cloth(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass, float tk,
                 float tc, float sk, float sc, float bk, float bc, const uint32_t* pins, uint64_t npins,
                 MeshTopo& out, std::string& err);
-// add_strut: rest length from `cur_pos` (3n floats, the points' current positions).
-int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, std::string& err);
+// add_strut: rest length from the points' current positions, read at
+// cur_pos[stride * i + 0..2].
+int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, size_t stride,
+              std::string& err);
 
 // Strut::new's length scaling: NOMINAL_STRUT_LENGTH / length * nominal (springy_mesh.rs:83-84).
 inline float scaled(float nominal, float length) { return 1.0f / length * nominal; }

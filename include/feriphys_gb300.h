@@ -100,6 +100,12 @@ int fgb_mesh_add_strut(fgb_mesh* m, uint32_t a, uint32_t b, float stiffness, flo
 /* SpringyMesh::add_pin -- springy_mesh.rs:415-417. */
 int fgb_mesh_add_pin(fgb_mesh* m, uint32_t index);
 
+/* add_strut / add_pin applied n times in order (one call for large meshes;
+ * same result as the loop). */
+int fgb_mesh_add_struts(fgb_mesh* m, const uint32_t* a, const uint32_t* b, const float* stiffness,
+                        const float* damping, uint64_t n);
+int fgb_mesh_add_pins(fgb_mesh* m, const uint32_t* index, uint64_t n);
+
 /* Counts: out[0] points, out[1] struts, out[2] faces, out[3] pins. */
 int fgb_mesh_counts(const fgb_mesh* m, uint64_t out[4]);
 
@@ -181,6 +187,12 @@ int fgb_sim_get_config(const fgb_sim* s, fgb_config* out);
 /* Simulation::step repeated n_steps times -- springy/simulation.rs:27-45.
  * Asynchronous: returns once the launches are queued. */
 int fgb_sim_step(fgb_sim* s, uint64_t n_steps);
+
+/* Issue the simulation's work (every mesh) on the caller's CUDA stream
+ * (a cudaStream_t passed as void*); NULL returns to the meshes' own streams.
+ * Extension with no reference counterpart: lets a host application order the
+ * step with its own GPU work and time it with its own events. */
+int fgb_sim_set_stream(fgb_sim* s, void* stream);
 
 /* Simulation::get_timestep -- springy/simulation.rs:47-49, as
  * Duration::from_secs_f32(dt).as_secs_f64(). */

@@ -84,12 +84,15 @@ def _declare(l):
         "oracle_mesh_free": (I, [P]),
         "oracle_mesh_add_strut": (I, [P, U64, U64, F, F]),
         "oracle_mesh_add_pin": (I, [P, U64]),
+        "oracle_mesh_add_struts": (I, [P, P, P, P, P, U64]),
+        "oracle_mesh_add_pins": (I, [P, P, U64]),
         "oracle_mesh_counts": (I, [P, P]),
         "oracle_mesh_get_points_f32": (I, [P, P]),
         "oracle_mesh_get_points_f64": (I, [P, P]),
         "oracle_mesh_set_points_f32": (I, [P, P]),
         "oracle_mesh_get_struts": (I, [P, P, P, P]),
         "oracle_mesh_get_faces": (I, [P, P, P]),
+        "oracle_mesh_set_strut_params": (I, [P, P, P]),
         "oracle_mesh_get_pins": (I, [P, P]),
         "oracle_mesh_face_normal": (I, [P, U64, P]),
         "oracle_mesh_face_angle": (I, [P, U64, I, P]),
@@ -203,6 +206,19 @@ class SpringyMesh:
     def add_pin(self, i):
         _ck(lib().oracle_mesh_add_pin(self._h, i))
 
+    def add_struts(self, pairs, k, c):
+        pairs = np.asarray(pairs, np.uint32).reshape(-1, 2)
+        n = len(pairs)
+        a = np.ascontiguousarray(pairs[:, 0])
+        b = np.ascontiguousarray(pairs[:, 1])
+        kk = np.ascontiguousarray(np.broadcast_to(np.asarray(k, np.float32), (n,)))
+        cc = np.ascontiguousarray(np.broadcast_to(np.asarray(c, np.float32), (n,)))
+        _ck(lib().oracle_mesh_add_struts(self._h, _ptr(a), _ptr(b), _ptr(kk), _ptr(cc), n))
+
+    def add_pins(self, pins):
+        p = _u32(pins)
+        _ck(lib().oracle_mesh_add_pins(self._h, _ptr(p), p.size))
+
     def counts(self):
         out = np.zeros(4, np.uint64)
         _ck(lib().oracle_mesh_counts(self._h, _ptr(out)))
@@ -234,6 +250,11 @@ class SpringyMesh:
         fc = np.zeros((s, 2), np.int64)
         _ck(lib().oracle_mesh_get_struts(self._h, _ptr(kcl), _ptr(ab), _ptr(fc)))
         return kcl, ab, fc
+
+    def set_strut_params(self, k, c):
+        k = _f32(k)
+        c = _f32(c)
+        _ck(lib().oracle_mesh_set_strut_params(self._h, _ptr(k), _ptr(c)))
 
     def get_faces(self):
         f = self.counts()[2]

@@ -713,6 +713,23 @@ int oracle_mesh_add_strut(void* h, uint64_t a, uint64_t b, float k, float c) {
   })
 }
 
+int oracle_mesh_add_struts(void* h, const uint32_t* a, const uint32_t* b, const float* k, const float* c, uint64_t n) {
+  ORACLE_TRY({
+    auto* m = static_cast<MeshH*>(h);
+    if (m->prec != 32) throw std::invalid_argument("add_strut on a widened mesh");
+    for (uint64_t i = 0; i < n; ++i) m->m32->add_strut(a[i], b[i], k[i], c[i]);
+  })
+}
+
+int oracle_mesh_add_pins(void* h, const uint32_t* p, uint64_t n) {
+  ORACLE_TRY({
+    auto* m = static_cast<MeshH*>(h);
+    for (uint64_t i = 0; i < n; ++i) {
+      if (m->prec == 32) m->m32->add_pin(p[i]); else m->m64->add_pin(p[i]);
+    }
+  })
+}
+
 int oracle_mesh_add_pin(void* h, uint64_t i) {
   ORACLE_TRY({
     auto* m = static_cast<MeshH*>(h);
@@ -780,6 +797,19 @@ int oracle_mesh_get_struts(void* h, float* kcl, uint64_t* ab, int64_t* faces) {
       if (kcl) { kcl[3 * i] = st[i].stiffness; kcl[3 * i + 1] = st[i].damping; kcl[3 * i + 2] = st[i].length; }
       if (ab) { ab[2 * i] = st[i].a; ab[2 * i + 1] = st[i].b; }
       if (faces) { faces[2 * i] = st[i].f0; faces[2 * i + 1] = st[i].f1; }
+    }
+  })
+}
+
+// Mirror of the library's fgb_mesh_set_strut_params extension: replace the
+// (already length-scaled) per-strut stiffness and damping in strut order.
+int oracle_mesh_set_strut_params(void* h, const float* k, const float* c) {
+  ORACLE_TRY({
+    auto* m = static_cast<MeshH*>(h);
+    if (m->prec != 32) throw std::invalid_argument("f32 mesh expected");
+    for (size_t i = 0; i < m->m32->struts.size(); ++i) {
+      m->m32->struts[i].stiffness = k[i];
+      m->m32->struts[i].damping = c[i];
     }
   })
 }
