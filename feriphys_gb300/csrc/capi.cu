@@ -563,25 +563,20 @@ int fgb_mesh_set_points(fgb_mesh* m, const float* in) {
     m->state_on_device = false;
     return FGB_OK;
   }
-  // Device-resident: DMA the raw points and convert on the device.
+  // Device-resident: DMA the raw points and convert on the device; the
+  // accumulated forces go to the force buffer (read once by the next step).
   FGB_CUDA(cudaSetDevice(m->device));
   FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
-  bool any_force = false;
-  for (size_t i = 0; i < n && !any_force; ++i)
-    any_force = in[10 * i + 7] != 0.0f || in[10 * i + 8] != 0.0f || in[10 * i + 9] != 0.0f ||
-                std::signbit(in[10 * i + 7]) || std::signbit(in[10 * i + 8]) || std::signbit(in[10 * i + 9]);
+  if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * n));
   FGB_CUDA(cudaMemcpyAsync(m->d_io, in, 10 * sizeof(float) * n, cudaMemcpyHostToDevice, m->stream));
-  void* F = nullptr;
-  if (any_force) {
-    if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * n));
-    F = m->force;
-  }
   if (m->precision == 64)
-    FGB_CUDA((fgb::launch_unpack<double>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], F, m->stream)));
+    FGB_CUDA((fgb::launch_unpack<double>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
+                                         m->stream)));
   else
-    FGB_CUDA((fgb::launch_unpack<float>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], F, m->stream)));
+    FGB_CUDA((fgb::launch_unpack<float>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
+                                        m->stream)));
   FGB_CUDA(cudaStreamSynchronize(m->stream));
-  m->has_force = any_force;
+  m->has_force = true;
   m->staged = false;
   return FGB_OK;
 }
@@ -876,8 +871,8 @@ int fgb_sim_synchronize(fgb_sim* s, int* nonfinite) {
 
 int fgb_sim_destroy(fgb_sim* s) {
   if (!s) return FGB_OK;
-  for (fgb_mesh* m : s->meshes)
-    if (m->stream) cudaStreamSynchronize(m->stream);
+  // The meshes may already be destroyed: touch none of them.  cudaFree waits
+  // for in-flight work that reads the obstacle faces.
   dfree(s->d_faces);
   delete s;
   return FGB_OK;

@@ -176,7 +176,8 @@ int fgb_collidable_destroy(fgb_obstacle* o);
 
 /* Simulation::new -- springy/simulation.rs:17-25 (starts from
  * Config::default()).  The simulation borrows the meshes and obstacles:
- * destroy it before them. */
+ * step it only while they live.  fgb_sim_destroy never touches them, so the
+ * handles may be destroyed in any order. */
 int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
                 fgb_sim** out);
 

@@ -43,17 +43,22 @@ def both(scene, fgb, orc, W, path=0):
     return g, o
 
 
-def compare_steps(g, o, steps, tol, every=1):
+def compare_steps(g, o, steps, tol, reset=True):
+    """Step both sides `steps` times.  With reset, the GPU state is set to the
+    oracle's before every step, so each step is checked on identical input
+    (the per-step bar); without it the trajectories drift freely."""
     gsim, gm, _ = g
     osim, om, _ = o
     worst = 0.0
-    for s in range(0, steps, every):
-        gsim.step(every)
-        osim.step(every)
+    for s in range(steps):
+        if reset:
+            gm.set_points(om.get_points())
+        gsim.step(1)
+        osim.step(1)
         gp, op = gm.get_points(), om.get_points()
         e = max(rel(gp[:, 1:4], op[:, 1:4]), rel(gp[:, 4:7], op[:, 4:7]))
         assert np.isfinite(op).all()
-        assert e <= tol, "step %d: relative error %.3g > %.3g" % (s + every, e, tol)
+        assert e <= tol, "step %d: relative error %.3g > %.3g" % (s + 1, e, tol)
         worst = max(worst, e)
     return worst
 
@@ -62,7 +67,17 @@ def compare_steps(g, o, steps, tol, every=1):
 def test_c0_per_step(fgb, orc, W, path):
     g, o = both(W.c0(), fgb, orc, W, path)
     assert g[1].get_path() == path
-    compare_steps(g, o, 60, PER_STEP_TOL)
+    worst = compare_steps(g, o, 120, PER_STEP_TOL)
+    print("c0 path %d: worst per-step relative error %.3g" % (path, worst))
+
+
+def test_c0_free_trajectory(fgb, orc, W):
+    # Without resets the GPU and oracle trajectories separate only through
+    # atan2f's last bit; at the configured dt=1/600 explicit Euler is
+    # unstable, which amplifies that, so the bar here is the long-horizon one.
+    g, o = both(W.c0(), fgb, orc, W)
+    worst = compare_steps(g, o, 100, LONG_TOL, reset=False)
+    print("c0 free trajectory: worst relative error over 100 steps %.3g" % worst)
 
 
 @pytest.mark.parametrize("path", [1, 2])
@@ -137,7 +152,7 @@ def test_collisions_plane_and_sphere(fgb, orc, W, path):
         moved_up += int((op[:, 5] > 0).sum())
         assert rel(gp[:, 1:4], op[:, 1:4]) <= PER_STEP_TOL, s
         assert rel(gp[:, 4:7], op[:, 4:7]) <= PER_STEP_TOL, s
-        # reset both to the oracle state so every step is checked on identical input
+        # continue both from the oracle state so every step is checked on identical input
         g[1].set_points(op)
     assert moved_up > 0  # collisions actually happened
 
@@ -174,7 +189,8 @@ def test_general_mesh(fgb, orc, W, integration):
     rng = np.random.default_rng(3)
     pos, idx = _random_mesh(rng)
     pairs = idx[:12].reshape(-1, 2)
-    kc = np.abs(rng.normal(1.0, 0.2, (len(pairs), 2))).astype(np.float32)
+    # nominal (k, c) overrides: effective k ~ 160-320 N/m, c ~ 0.2-0.6 N.s/m on 5 cm struts
+    kc = np.stack([rng.uniform(8.0, 16.0, len(pairs)), rng.uniform(0.01, 0.03, len(pairs))], 1).astype(np.float32)
     cfg = W.cloth_config(1.0 / 1200.0, integration)
     g = fgb.SpringyMesh.new(pos, idx, 0.81, 12.0, 0.02, (pairs, kc))
     o = orc.SpringyMesh.new(pos, idx, 0.81, 12.0, 0.02, (pairs, kc))
