@@ -190,7 +190,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general gather, 2 grid stencil")
+    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general gather, 2 tiled grid, 3 untiled grid")
     ap.add_argument("--probe", action="store_true", help="report the first step whose state is non-finite")
     args = ap.parse_args()
 
@@ -334,7 +334,7 @@ def main():
                                        "initial state" % (args.n, args.n, n_vert, n_struts, n_faces, args.rollout),
                            "l2": "flushed (256 MB write) before every timed step",
                            "parallelism": "replicas" if world > 1 else "single GPU",
-                           "path": ["?", "general gather", "grid stencil"][mesh.get_path()]},
+                           "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
                 "device": torch.cuda.get_device_name()}

@@ -129,6 +129,7 @@ def _declare(l):
         "fgb_sim_get_config": (I, [P, cfg]),
         "fgb_sim_step": (I, [P, U64]),
         "fgb_sim_set_stream": (I, [P, P]),
+        "fgb_sim_set_collision_broadphase": (I, [P, I]),
         "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
         "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
         "fgb_sim_destroy": (I, [P]),
@@ -410,6 +411,10 @@ class Simulation:
         simulated seconds of one step like the reference's Duration."""
         _check(_lib().fgb_sim_step(self._h, int(n_steps)))
         return self.get_timestep()
+
+    def set_collision_broadphase(self, enabled: bool):
+        """True (default): exact broad phase; False: test every obstacle face."""
+        _check(_lib().fgb_sim_set_collision_broadphase(self._h, 1 if enabled else 0))
 
     def set_stream(self, stream_handle):
         """Issue every mesh's work on an external cudaStream_t (an integer

@@ -10,9 +10,10 @@
 #include <utility>
 #include <vector>
 
-#include "../../include/feriphys_gb300.h"
+#include "feriphys_gb300.h"
 #include "kernels.h"
 #include "mesh_build.h"
+#include "obstacle_accel.h"
 #include "physics.cuh"
 #include "state_io.h"
 
@@ -69,6 +70,7 @@ struct fgb_mesh {
   MeshTopo topo;
   int device = 0;
   int path_req = 0;      // 0 auto, 1 general, 2 grid
+  int grid_variant = 0;  // 0 tiled grid kernel, 1 per-vertex grid kernel
   int precision = 32;    // 32 or 64
   int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
   cudaStream_t stream = nullptr;      // the stream all work of this mesh is issued on
@@ -118,6 +120,9 @@ struct fgb_sim {
   fgb::ObsFace* d_faces = nullptr;
   int n_faces = 0;
   bool faces_uploaded = false;
+  bool broadphase = true;
+  fgb::ObsAccel accel{};  // device broad phase (pointers into d_accel)
+  int* d_accel = nullptr;
 };
 
 namespace {
@@ -315,8 +320,11 @@ int ensure_device(fgb_mesh* m) {
   return FGB_OK;
 }
 
-fgb::StepConsts make_consts(const fgb_config& cfg, const fgb::ObsFace* faces, int n_faces, unsigned* flags) {
+fgb::StepConsts make_consts(const fgb_config& cfg, const fgb::ObsFace* faces, int n_faces, unsigned* flags,
+                            const fgb::ObsAccel* accel = nullptr) {
   fgb::StepConsts c;
+  std::memset(&c, 0, sizeof(c));
+  if (accel) c.accel = *accel;
   c.integration = cfg.integration;
   c.dt = cfg.dt;
   c.dt_duration = fgb::duration_roundtrip(cfg.dt);
@@ -348,7 +356,7 @@ int step_mesh(fgb_mesh* m, const fgb::StepConsts& c) {
   const int nxt = m->cur ^ 1;
   const void* F = m->has_force ? m->force : nullptr;
   if (m->active_path == 2) {
-    fgb::GridTopo g{int(m->topo.rows), int(m->topo.cols), m->d_grid};
+    fgb::GridTopo g{int(m->topo.rows), int(m->topo.cols), m->d_grid, m->grid_variant};
     FGB_CUDA(fgb::launch_step_grid(g, static_cast<const float4*>(m->pos[m->cur]),
                                    static_cast<const float4*>(m->vel[m->cur]), static_cast<const float4*>(F),
                                    static_cast<float4*>(m->pos[nxt]), static_cast<float4*>(m->vel[nxt]), c,
@@ -608,8 +616,9 @@ int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices) {
 }
 
 int fgb_mesh_set_path(fgb_mesh* m, int path) {
-  if (!m || path < 0 || path > 2) return fail(FGB_EINVAL, "path must be 0, 1 or 2");
-  m->path_req = path;
+  if (!m || path < 0 || path > 3) return fail(FGB_EINVAL, "path must be 0, 1, 2 or 3");
+  m->path_req = path == 3 ? 2 : path;
+  m->grid_variant = path == 3 ? 1 : 0;
   m->topo_dirty = true;
   return FGB_OK;
 }
@@ -825,12 +834,44 @@ int fgb_sim_step(fgb_sim* s, uint64_t n_steps) {
       FGB_CUDA(dalloc(s->d_faces, s->faces.size() * sizeof(fgb::ObsFace)));
       FGB_CUDA(cudaMemcpy(s->d_faces, s->faces.data(), s->faces.size() * sizeof(fgb::ObsFace),
                           cudaMemcpyHostToDevice));
+      std::vector<int> first, count;
+      int base = 0;
+      for (fgb_obstacle* o : s->obstacles) {
+        first.push_back(base);
+        count.push_back(int(o->faces.size()));
+        base += int(o->faces.size());
+      }
+      fgb::AccelHost a;
+      fgb::build_obstacle_accel(s->faces, first, count, a);
+      const size_t n_off = a.cell_off.size(), n_cf = a.cell_faces.size(), n_al = a.always.size();
+      const size_t n_grid_ints = a.grids.size() * sizeof(fgb::ObsGrid3) / sizeof(int);
+      FGB_CUDA(dalloc(s->d_accel, (n_off + n_cf + n_al + n_grid_ints + 4) * sizeof(int)));
+      FGB_CUDA(cudaMemcpy(s->d_accel, a.cell_off.data(), n_off * sizeof(int), cudaMemcpyHostToDevice));
+      FGB_CUDA(cudaMemcpy(s->d_accel + n_off, a.cell_faces.data(), n_cf * sizeof(int), cudaMemcpyHostToDevice));
+      FGB_CUDA(cudaMemcpy(s->d_accel + n_off + n_cf, a.always.data(), n_al * sizeof(int), cudaMemcpyHostToDevice));
+      // grid descriptors last, 16-byte aligned
+      const size_t gofs = (n_off + n_cf + n_al + 3) & ~size_t(3);
+      FGB_CUDA(cudaMemcpy(s->d_accel + gofs, a.grids.data(), a.grids.size() * sizeof(fgb::ObsGrid3),
+                          cudaMemcpyHostToDevice));
+      s->accel.cell_off = s->d_accel;
+      s->accel.cell_faces = s->d_accel + n_off;
+      s->accel.always = s->d_accel + n_off + n_cf;
+      s->accel.grids = reinterpret_cast<const fgb::ObsGrid3*>(s->d_accel + gofs);
+      s->accel.n_grids = int(a.grids.size());
     }
     s->faces_uploaded = true;
   }
+  s->accel.enabled = (s->broadphase && s->d_accel) ? 1 : 0;
   for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_device(m));
   for (uint64_t k = 0; k < n_steps; ++k)
-    for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags)));
+    for (fgb_mesh* m : s->meshes)
+      FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags, &s->accel)));
+  return FGB_OK;
+}
+
+int fgb_sim_set_collision_broadphase(fgb_sim* s, int enabled) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  s->broadphase = enabled != 0;
   return FGB_OK;
 }
 
@@ -874,6 +915,7 @@ int fgb_sim_destroy(fgb_sim* s) {
   // The meshes may already be destroyed: touch none of them.  cudaFree waits
   // for in-flight work that reads the obstacle faces.
   dfree(s->d_faces);
+  dfree(s->d_accel);
   delete s;
   return FGB_OK;
 }

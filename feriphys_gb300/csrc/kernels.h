@@ -24,6 +24,7 @@ struct GeneralTopo {
 struct GridTopo {
   int rows, cols;
   const float4* params;
+  int variant;  // 0: shared-memory tiles, 1: one thread per vertex reading global memory
 };
 
 template <class T>

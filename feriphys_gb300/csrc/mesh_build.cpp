@@ -6,7 +6,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "../../include/feriphys_gb300.h"
+#include "feriphys_gb300.h"
 
 namespace fgb {
 

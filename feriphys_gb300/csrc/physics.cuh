@@ -9,6 +9,7 @@
 #pragma once
 
 #include "devmath.cuh"
+#include "fastdiv.cuh"
 #include "step_consts.h"
 
 namespace fgb {
@@ -50,32 +51,54 @@ __device__ __forceinline__ T face_corner_weight(V3<T> x0, V3<T> x1, V3<T> x2, in
   return a / T(kPiF32);
 }
 
+// F / m componentwise, exactly as IEEE division; the f32 form shares one
+// correctly rounded reciprocal of m (fastdiv.cuh).
+struct MassDiv {
+  float m, y;
+  bool fast;
+};
+__device__ __forceinline__ MassDiv mass_div(float m) {
+  const bool fast = rcp_usable(m);
+  return {m, fast ? __frcp_rn(m) : 0.0f, fast};
+}
+__device__ __forceinline__ V3<float> div_mass(V3<float> F, float m, const MassDiv& d) {
+  if (d.fast && m == d.m && !signbit(m) == !signbit(d.m))
+    return {div_known_rcp(F.x, d.m, d.y), div_known_rcp(F.y, d.m, d.y), div_known_rcp(F.z, d.m, d.y)};
+  return F / m;
+}
+struct MassDivD {
+  double m;
+};
+__device__ __forceinline__ MassDivD mass_div(double m) { return {m}; }
+__device__ __forceinline__ V3<double> div_mass(V3<double> F, double m, const MassDivD&) { return F / m; }
+
 // State integration of one point with frozen force F.  m' = m + 0*h and
 // F' = F + 0*h are kept (they only differ from m, F in the sign of zero).
 template <class T>
 __device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V3<T> v, V3<T> F, T m, V3<T>& np,
                                                 V3<T>& nv, V3<T>& nF) {
   const V3<T> z3{T(0), T(0), T(0)};
+  const auto md = mass_div(m);
   if (integration == 0) {  // state.rs:75-83
-    const V3<T> a = F / m;
+    const V3<T> a = div_mass(F, m, md);
     np = p + v * h;
     nv = v + a * h;
     nF = F + z3 * h;
   } else {  // state.rs:86-106: k1..k4 share the carried F, so only v stages differ
     const T hh = h * T(0.5);
-    const V3<T> a1 = F / m;
+    const V3<T> a1 = div_mass(F, m, md);
     const V3<T> F2 = F + z3 * hh;
     const T m2 = m + T(0) * hh;
     const V3<T> v2 = v + a1 * hh;
-    const V3<T> a2 = F2 / m2;
+    const V3<T> a2 = div_mass(F2, m2, md);
     const V3<T> F3 = F + z3 * hh;
     const T m3 = m + T(0) * hh;
     const V3<T> v3 = v + a2 * hh;
-    const V3<T> a3 = F3 / m3;
+    const V3<T> a3 = div_mass(F3, m3, md);
     const V3<T> F4 = F + z3 * h;
     const T m4 = m + T(0) * h;
     const V3<T> v4 = v + a3 * h;
-    const V3<T> a4 = F4 / m4;
+    const V3<T> a4 = div_mass(F4, m4, md);
     const T h6 = h / T(6), h3 = h / T(3);
     np = p + (((h6 * v + h3 * v2) + h3 * v3) + h6 * v4);
     nv = v + (((h6 * a1 + h3 * a2) + h3 * a3) + h6 * a4);
@@ -84,28 +107,25 @@ __device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V
   }
 }
 
-// One obstacle face as stored on the device: v0 (w = drop axis 0/1/2 as
-// float bits), v1, v2, unit normal (computed on the host exactly as
-// collidable_mesh.rs:41-43 does).
-struct ObsFace {
-  float4 v0, v1, v2, n;
-};
-
 // The crossing test of one face (collidable_mesh.rs:107-145): signs of the
 // plane distances differ and the projected point lies inside the triangle.
+// The triangle's other vertices are only loaded once the plane is crossed.
 template <class T>
-__device__ __forceinline__ bool face_hit(const ObsFace& F, V3<T> op, V3<T> np, T dtd, T& d_old, T& d_new) {
-  const V3<T> v0{T(F.v0.x), T(F.v0.y), T(F.v0.z)};
-  const V3<T> n{T(F.n.x), T(F.n.y), T(F.n.z)};
+__device__ __forceinline__ bool face_hit(const ObsFace* __restrict__ Fp, V3<T> op, V3<T> np, T dtd, T& d_old,
+                                         T& d_new) {
+  const float4 fv0 = Fp->v0, fn = Fp->n;
+  const V3<T> v0{T(fv0.x), T(fv0.y), T(fv0.z)};
+  const V3<T> n{T(fn.x), T(fn.y), T(fn.z)};
   d_old = dot(op - v0, n);
   d_new = dot(np - v0, n);
   if (signbit(d_old) == signbit(d_new)) return false;
   const V3<T> ovel = (np - op) / dtd;
   const T fr = d_old / (d_old - d_new);
   const V3<T> cp = op + (dtd * fr) * ovel;
-  const V3<T> v1{T(F.v1.x), T(F.v1.y), T(F.v1.z)};
-  const V3<T> v2{T(F.v2.x), T(F.v2.y), T(F.v2.z)};
-  const int axis = __float_as_int(F.v0.w);
+  const float4 fv1 = Fp->v1, fv2 = Fp->v2;
+  const V3<T> v1{T(fv1.x), T(fv1.y), T(fv1.z)};
+  const V3<T> v2{T(fv2.x), T(fv2.y), T(fv2.z)};
+  const int axis = __float_as_int(fv0.w);
   V3<T> a = v0, b = v1, c = v2, p = cp;
   if (axis == 0) { a.x = T(0); b.x = T(0); c.x = T(0); p.x = T(0); }
   else if (axis == 1) { a.y = T(0); b.y = T(0); c.y = T(0); p.y = T(0); }
@@ -118,9 +138,11 @@ __device__ __forceinline__ bool face_hit(const ObsFace& F, V3<T> op, V3<T> np, T
 
 // Collision response (springy_mesh.rs:444-480) for a hit on face F.
 template <class T>
-__device__ __forceinline__ void collision_response(const ObsFace& F, T d_old, T d_new, V3<T> op, V3<T> ov, V3<T> oF,
-                                                   T om, T dt, T e, T mu, V3<T>& np, V3<T>& nv) {
-  const V3<T> n{T(F.n.x), T(F.n.y), T(F.n.z)};
+__device__ __forceinline__ void collision_response(const ObsFace* __restrict__ Fp, T d_old, T d_new, V3<T> op,
+                                                   V3<T> ov, V3<T> oF, T om, T dt, T e, T mu, V3<T>& np,
+                                                   V3<T>& nv) {
+  const float4 fn = Fp->n;
+  const V3<T> n{T(fn.x), T(fn.y), T(fn.z)};
   const T fr = d_old / (d_old - d_new);
   const V3<T> cp = op + (dt * fr) * ov;
   const V3<T> vc = ov + ((dt * fr) * oF) / om;
@@ -137,16 +159,108 @@ __device__ __forceinline__ void collision_response(const ObsFace& F, T d_old, T 
 // First hit over the flattened obstacle faces, then the response.  Returns
 // true when the point collided.
 template <class T>
-__device__ __forceinline__ bool collide_point(const ObsFace* __restrict__ faces, int n_faces, V3<T> op, V3<T> ov,
-                                              V3<T> oF, T om, V3<T>& np, V3<T>& nv, const StepConsts& c) {
+__device__ __forceinline__ bool collide_point_all(const ObsFace* __restrict__ faces, int n_faces, V3<T> op, V3<T> ov,
+                                                  V3<T> oF, T om, V3<T>& np, V3<T>& nv, const StepConsts& c) {
   const T dtd = T(c.dt_duration);
   for (int f = 0; f < n_faces; ++f) {
-    const ObsFace F = faces[f];
     T d_old, d_new;
-    if (face_hit(F, op, np, dtd, d_old, d_new)) {
-      collision_response(F, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
+    if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
+      collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
       return true;
     }
+  }
+  return false;
+}
+
+// Margin of the query box: the computed crossing point can leave the
+// segment's box by a few ulps of the step and of the coordinates.
+__device__ __forceinline__ float query_slack(float a, float b) {
+  return 1e-5f * fabsf(a - b) + 1e-5f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f;
+}
+
+template <class T>
+__device__ __forceinline__ bool test_faces_from(const ObsFace* __restrict__ faces, const int* __restrict__ list_a,
+                                                int ba, int ea, const int* __restrict__ list_b, int bb, int eb,
+                                                V3<T> op, V3<T> ov, V3<T> oF, T om, V3<T>& np, V3<T>& nv,
+                                                const StepConsts& c) {
+  // visit the union of two ascending lists in ascending order
+  const T dtd = T(c.dt_duration);
+  while (ba < ea || bb < eb) {
+    const int fa = ba < ea ? list_a[ba] : 0x7fffffff;
+    const int fb = bb < eb ? list_b[bb] : 0x7fffffff;
+    int f;
+    if (fa <= fb) { f = fa; ++ba; } else { f = fb; ++bb; }
+    T d_old, d_new;
+    if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
+      collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
+      return true;
+    }
+  }
+  return false;
+}
+
+// First hit with the broad phase: obstacles in order; within one, the faces
+// of the query's cell merged with the always-tested faces in ascending
+// index.  The narrow test is the same face_hit as the full search, so the
+// result is identical.
+template <class T>
+__device__ __forceinline__ bool collide_point(const ObsFace* __restrict__ faces, int n_faces, V3<T> op, V3<T> ov,
+                                              V3<T> oF, T om, V3<T>& np, V3<T>& nv, const StepConsts& c) {
+  if (n_faces == 0) return false;
+  const ObsAccel& A = c.accel;
+  if (!A.enabled || !finite3(op) || !finite3(np))
+    return collide_point_all(faces, n_faces, op, ov, oF, om, np, nv, c);
+  float lo[3], hi[3];
+  {
+    const float o3[3] = {float(op.x), float(op.y), float(op.z)};
+    const float n3[3] = {float(np.x), float(np.y), float(np.z)};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float s = query_slack(o3[d], n3[d]);
+      lo[d] = fminf(o3[d], n3[d]) - s;
+      hi[d] = fmaxf(o3[d], n3[d]) + s;
+    }
+  }
+  for (int k = 0; k < A.n_grids; ++k) {
+    const ObsGrid3& g = A.grids[k];
+    int cb = 0, ce = 0;
+    bool all = false;
+    if (g.n[0] > 0 && hi[0] >= g.lo[0] && lo[0] <= g.hi[0] && hi[1] >= g.lo[1] && lo[1] <= g.hi[1] &&
+        hi[2] >= g.lo[2] && lo[2] <= g.hi[2]) {
+      int idx[3];
+      bool fits = true;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        int i = int(floorf((0.5f * (lo[d] + hi[d]) - g.lo[d]) * g.inv[d]));
+        i = min(max(i, 0), g.n[d] - 1);
+        const float c0 = g.lo[d] + float(i) * g.cell[d] - g.slack;
+        const float c1 = g.lo[d] + float(i + 1) * g.cell[d] + g.slack;
+        fits = fits && lo[d] >= c0 && hi[d] <= c1;
+        idx[d] = i;
+      }
+      if (fits) {
+        const int cell = g.off_base + (idx[0] * g.n[1] + idx[1]) * g.n[2] + idx[2];
+        cb = A.cell_off[cell];
+        ce = A.cell_off[cell + 1];
+      } else {
+        all = true;
+      }
+    }
+    if (all) {  // the box does not fit one cell: test every face of this obstacle in order
+      const T dtd = T(c.dt_duration);
+      for (int f = g.face_base; f < g.face_base + g.n_faces; ++f) {
+        T d_old, d_new;
+        if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
+          collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction),
+                             np, nv);
+          return true;
+        }
+      }
+      continue;
+    }
+    if (test_faces_from(faces, A.cell_faces, cb, ce, A.always, g.always_base, g.always_base + g.n_always, op, ov, oF,
+                        om, np, nv, c))
+      return true;
   }
   return false;
 }

@@ -3,8 +3,39 @@
 #pragma once
 
 #include <stdint.h>
+#include <vector_types.h>
 
 namespace fgb {
+
+// One obstacle face as stored on the device: v0 (w = drop axis 0/1/2 as
+// float bits), v1, v2, unit normal (computed on the host exactly as
+// collidable_mesh.rs:41-43 does).
+struct ObsFace {
+  float4 v0, v1, v2, n;
+};
+
+// Broad-phase grid of one obstacle (see obstacle_accel.h): a uniform 3D grid
+// over the union of its faces' acceptance regions; each cell lists, in
+// ascending order, the faces whose region meets the cell grown by 2*slack.
+struct ObsGrid3 {
+  float lo[3], hi[3];  // union of the faces' regions (outward-rounded)
+  float cell[3];       // cell size
+  float inv[3];        // 1 / cell size
+  float slack;         // a query box must fit its cell grown by this
+  int n[3];            // cells per axis (0: no bounded face)
+  int off_base;        // first entry of this grid in cell_off
+  int face_base, n_faces;     // the obstacle's faces in the flattened order
+  int always_base, n_always;  // faces tested for every query (in `always`)
+};
+
+struct ObsAccel {
+  int enabled;
+  int n_grids;
+  const ObsGrid3* grids;
+  const int* cell_off;
+  const int* cell_faces;
+  const int* always;
+};
 
 struct StepConsts {
   int integration;     // 0 Euler, 1 Rk4 (state.rs:4-8)
@@ -19,6 +50,7 @@ struct StepConsts {
   int n_obstacle_faces;
   const void* obstacle_faces;  // ObsFace[n_obstacle_faces], flattened obstacle order
   unsigned* flags;             // bit 0: a stepped vertex went non-finite
+  ObsAccel accel;              // broad phase over obstacle_faces (enabled = 0: test all faces)
 };
 
 }  // namespace fgb

@@ -6,6 +6,7 @@
 // order of the reference's scatter loops (strut ids ascending, then face ids
 // ascending -- checked on the host against the real ids before this kernel is
 // chosen), so the result is bit-identical to the general gather.
+#include "fastdiv.cuh"
 #include "grid_order.h"
 #include "kernels.h"
 #include "physics.cuh"
@@ -96,13 +97,509 @@ __global__ void __launch_bounds__(256) k_step_grid_v1(int R, int C, const float4
   if (__any_sync(__activemask(), bad) && bad && c.flags) atomicOr(c.flags, 1u);
 }
 
+
+// ---------------------------------------------------------------------------
+// Tiled kernel.  A CTA owns a TW x TH tile of vertices.  It stages the tile
+// plus a 2-vertex halo (binding struts reach 2 vertices) in shared memory,
+// computes every strut and face touching the tile once, and each thread then
+// gathers its vertex's terms from shared memory in the reference's order.
+// Binding struts come after all triangle struts in strut order, so they are
+// computed and summed in a second phase that reuses the same buffer; faces
+// come after all struts and use it a third time.
+
+// drag+lift (D) and the three corner weights angle_k / PI of one face.  The
+// corner angles reuse exact identities: |(x2-x0) x (x1-x0)| is bitwise
+// |(x1-x0) x (x2-x0)|, and x0-x1 = -(x1-x0), x1-x2 = -(x2-x1) exactly.
+__device__ __forceinline__ void face_terms(V3<float> x0, V3<float> x1, V3<float> x2, V3<float> v0, V3<float> v1,
+                                           V3<float> v2, V3<float> wind, float neg_cd, float neg_lift,
+                                           float4& Dw0, float2& w12) {
+  const V3<float> sum = (v0 + v1) + v2;
+  const V3<float> avg{div_known_rcp(sum.x, 3.0f, kRcp3), div_known_rcp(sum.y, 3.0f, kRcp3),
+                      div_known_rcp(sum.z, 3.0f, kRcp3)};
+  const V3<float> rv = avg - wind;
+  const V3<float> e1 = x1 - x0, e2 = x2 - x0, e3 = x2 - x1;
+  const V3<float> cr = cross(e1, e2);
+  const float mag = magnitude(cr);
+  const float area = mag / 2.0f;
+  const V3<float> n = cr * (1.0f / mag);
+  const float eff = area * fabsf(dot(n, rv));
+  const V3<float> drag = (neg_cd * eff) * rv;
+  const V3<float> lift = (neg_lift * eff) * (rv * magnitude(cross(n, rv)));
+  const V3<float> D = drag + lift;
+  const float a0 = atan2f(mag, dot(e2, e1));
+  const float a1 = atan2f(magnitude(cross(e1, e3)), -dot(e1, e3));
+  const float a2 = atan2f(magnitude(cross(e3, e2)), dot(e3, e2));
+  Dw0 = make_float4(D.x, D.y, D.z, div_known_rcp(a0, kPiF32, kRcpPi));
+  w12 = make_float2(div_known_rcp(a1, kPiF32, kRcpPi), div_known_rcp(a2, kPiF32, kRcpPi));
+}
+
+template <int TW, int TH>
+struct TileGeom {
+  static constexpr int EW = TW + 4, EH = TH + 4;  // staged region, origin (r0-2, c0-2)
+  // strut owner regions (row range x col range relative to (r0, c0))
+  static constexpr int KH_W = TW + 1, KH_H = TH;      // rows [0, TH), cols [-1, TW)
+  static constexpr int KV_W = TW, KV_H = TH + 1;      // rows [-1, TH), cols [0, TW)
+  static constexpr int KS_W = TW + 1, KS_H = TH + 1;  // rows [-1, TH), cols [-1, TW)
+  static constexpr int KBH_W = TW + 2, KBH_H = TH;    // rows [0, TH), cols [-2, TW)
+  static constexpr int KBV_W = TW, KBV_H = TH + 2;    // rows [-2, TH), cols [0, TW)
+  static constexpr int Q_W = TW + 1, Q_H = TH + 1;    // quads rows [-1, TH), cols [-1, TW)
+  static constexpr int N_KH = KH_W * KH_H, N_KV = KV_W * KV_H, N_KS = KS_W * KS_H;
+  static constexpr int N_TRI = N_KH + N_KV + N_KS;
+  static constexpr int N_KBH = KBH_W * KBH_H, N_KBV = KBV_W * KBV_H;
+  static constexpr int N_BIND = N_KBH + N_KBV;
+  static constexpr int N_Q = Q_W * Q_H;
+  // buffer in float4 units: struts need 2 (spring, damper), a quad needs
+  // 2 float4 + 2 float2 = 3 float4
+  static constexpr int BUF = (2 * N_TRI > 2 * N_BIND ? (2 * N_TRI > 3 * N_Q ? 2 * N_TRI : 3 * N_Q)
+                                                     : (2 * N_BIND > 3 * N_Q ? 2 * N_BIND : 3 * N_Q));
+};
+
+template <int TW, int TH>
+struct Interior {
+  static constexpr int OW = TW + 2, OH = TH + 2;  // owner grid: rows r0-2.., cols c0-2..
+  static constexpr int NO = OW * OH;
+  static constexpr int QW = TW + 1, QH = TH + 1;  // quads: rows r0-1.., cols c0-1..
+  static constexpr int NQ = QW * QH;
+  // bytes after the staged pos/vel: 5 strut kinds x (float4 (u, s1) + float s2), 3 float4 per quad
+  static constexpr int BYTES = 5 * NO * 20 + NQ * 48;
+};
+
+// Strut of the compact form: unit vector u and the spring/damper scalars
+// s1 = k(|d| - L), s2 = c (dv . u); the forces are s1*u and s2*u, which a
+// gathering thread forms itself (the same products, so the same bits).
+__device__ __forceinline__ void strut_compact(const float4* __restrict__ s_pos, const float4* __restrict__ s_vel,
+                                              int ia, int ib, float k, float cd, float L, float4* __restrict__ su,
+                                              float* __restrict__ s2) {
+  const V3<float> d = xyz<float>(s_pos[ib]) - xyz<float>(s_pos[ia]);
+  const float mag = magnitude(d);
+  const V3<float> u = d * (1.0f / mag);
+  const float s1 = k * (mag - L);
+  const float sd = cd * dot(xyz<float>(s_vel[ib]) - xyz<float>(s_vel[ia]), u);
+  *su = make_float4(u.x, u.y, u.z, s1);
+  *s2 = sd;
+}
+
+__device__ __forceinline__ void add_compact(V3<float>& F, float4 su, float s2, int role) {
+  const V3<float> u{su.x, su.y, su.z};
+  if (role == 0) {
+    F = F + su.w * u;
+    F = F + s2 * u;
+  } else {  // -1.0 * (s*u) == (-s)*u exactly
+    F = F + (-su.w) * u;
+    F = F + (-s2) * u;
+  }
+}
+
+__device__ __forceinline__ void quad_to(const float4* __restrict__ s_pos, const float4* __restrict__ s_vel, int e00,
+                                        int e01, int e10, int e11, V3<float> wind, float neg_cd, float neg_lift,
+                                        float4* __restrict__ qa, float4* __restrict__ qb, float4* __restrict__ qw) {
+  float4 a, b;
+  float2 wa, wb;
+  // A = (i+1, i+C, i), B = (i+1, i+C+1, i+C) for quad origin i
+  face_terms(xyz<float>(s_pos[e01]), xyz<float>(s_pos[e10]), xyz<float>(s_pos[e00]), xyz<float>(s_vel[e01]),
+             xyz<float>(s_vel[e10]), xyz<float>(s_vel[e00]), wind, neg_cd, neg_lift, a, wa);
+  face_terms(xyz<float>(s_pos[e01]), xyz<float>(s_pos[e11]), xyz<float>(s_pos[e10]), xyz<float>(s_vel[e01]),
+             xyz<float>(s_vel[e11]), xyz<float>(s_vel[e10]), wind, neg_cd, neg_lift, b, wb);
+  *qa = a;
+  *qb = b;
+  *qw = make_float4(wa.x, wa.y, wb.x, wb.y);
+}
+
+__device__ __forceinline__ void add_pair(V3<float>& F, const float4* __restrict__ pair, int role) {
+  const V3<float> sf = xyz<float>(pair[0]), df = xyz<float>(pair[1]);
+  if (role == 0) {
+    F = F + sf;
+    F = F + df;
+  } else {
+    F = F + (-1.0f * sf);
+    F = F + (-1.0f * df);
+  }
+}
+
+// One CTA = a TW x TH tile: TW*TH "main" threads (one per vertex) plus
+// HALO helper threads that compute the tile's halo struts and faces while
+// the main threads compute their own, so no thread does double work.
+// Tiles split into an interior rectangle [bx0, bx1] x [by0, by1] (every
+// neighbour of every tile vertex exists: fixed offsets, no checks) and the
+// ring of boundary tiles around it, launched as two kernels.
+struct TileSplit {
+  int tx, ty;          // tiles per row / column
+  int bx0, bx1, by0, by1;  // interior rectangle (empty when bx1 < bx0 or by1 < by0)
+};
+
+__device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, int& by) {
+  const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
+  if (!has_interior) {
+    bx = k % t.tx;
+    by = k / t.tx;
+    return;
+  }
+  const int top = t.by0 * t.tx;
+  if (k < top) {
+    bx = k % t.tx;
+    by = k / t.tx;
+    return;
+  }
+  k -= top;
+  const int bottom = (t.ty - 1 - t.by1) * t.tx;
+  if (k < bottom) {
+    bx = k % t.tx;
+    by = t.by1 + 1 + k / t.tx;
+    return;
+  }
+  k -= bottom;
+  const int per_row = t.bx0 + (t.tx - 1 - t.bx1);
+  by = t.by0 + k / per_row;
+  const int j = k % per_row;
+  bx = j < t.bx0 ? j : t.bx1 + 1 + (j - t.bx0);
+}
+
+template <int TW, int TH, int HALO, bool INTERIOR>
+__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, int C, TileSplit split,
+                                                                      const float4* __restrict__ planes,
+                                                                      const float4* __restrict__ pos,
+                                                                      const float4* __restrict__ vel,
+                                                                      const float4* __restrict__ force_in,
+                                                                      float4* __restrict__ pos_out,
+                                                                      float4* __restrict__ vel_out, StepConsts c) {
+  using G = TileGeom<TW, TH>;
+  using I = Interior<TW, TH>;
+  constexpr int NMAIN = TW * TH, NT = TW * TH + HALO;
+  static_assert(HALO == 2 * TW && TW + TH <= 40 && TW >= 32, "helper layout assumes a 32-wide tile, 64 helpers");
+  extern __shared__ float4 s_dyn[];
+  float4* s_pos = s_dyn;
+  float4* s_vel = s_dyn + G::EH * G::EW;
+  float4* s_buf = s_dyn + 2 * G::EH * G::EW;
+  const int n = R * C;
+  int bx, by;
+  if (INTERIOR) {
+    bx = split.bx0 + blockIdx.x;
+    by = split.by0 + blockIdx.y;
+  } else {
+    ring_tile(split, blockIdx.x, bx, by);
+  }
+  const int c0 = bx * TW, r0 = by * TH;
+  const int tid = threadIdx.x;
+  const V3<float> wind{c.wind[0], c.wind[1], c.wind[2]};
+  const float4* __restrict__ plane0 = planes;
+  const float4* __restrict__ plane1 = planes + n;
+  const float4* __restrict__ plane2 = planes + 2 * size_t(n);
+  const float4* __restrict__ plane3 = planes + 3 * size_t(n);
+
+  V3<float> F{c.force0[0], c.force0[1], c.force0[2]};
+  const int lr = tid / TW, lc = tid % TW;
+  const int r = r0 + lr, cc = c0 + lc;
+
+  if constexpr (INTERIOR) {
+    constexpr int EW = G::EW, OW = I::OW, NO = I::NO, QW = I::QW, NQ = I::NQ;
+    float4* s_su = s_buf;                                      // [5][NO]
+    float* s_s2 = reinterpret_cast<float*>(s_buf + 5 * NO);    // [5][NO]
+    float4* s_qa = reinterpret_cast<float4*>(s_s2 + 5 * NO);   // [NQ]
+    float4* s_qb = s_qa + NQ;
+    float4* s_qw = s_qb + NQ;
+    auto e = [](int rr, int ccl) { return (rr + 2) * EW + (ccl + 2); };  // tile-relative staged index
+    auto o = [](int rr, int ccl) { return (rr + 2) * OW + (ccl + 2); };  // tile-relative owner index
+    auto qi = [](int rr, int ccl) { return (rr + 1) * QW + (ccl + 1); };
+    // ---- stage positions/velocities; prefetch the strut constants this thread needs
+    for (int i = tid; i < G::EH * G::EW; i += NT) {
+      const int g = (r0 - 2 + i / G::EW) * C + (c0 - 2 + i % G::EW);
+      s_pos[i] = pos[g];
+      s_vel[i] = vel[g];
+    }
+    const int h = tid - NMAIN;
+    // Main threads: the five struts owned by their vertex and its quad.
+    // Helper lanes: up to three strut jobs (kind, owner) and at most one quad,
+    // laid out so a warp never runs two expensive branches one after another:
+    //   h in [0, 32):  owner (-1, h): vertical, shear, vertical binding; quad (-1, h)
+    //   h in [32, 64): vertical binding owned by (-2, h-32), plus
+    //     h in [32, 40): horizontal and shear owned by (h-32, -1); quad (h-32, -1)
+    //     h in [40, 48): horizontal bindings owned by (h-40, -2) and (h-40, -1)
+    //     h == 48:       shear owned by (-1, -1); quad (-1, -1)
+    float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
+    int job_kind[3] = {-1, -1, -1}, job_r[3] = {0, 0, 0}, job_c[3] = {0, 0, 0};
+    float job_k[3] = {0, 0, 0}, job_cd[3] = {0, 0, 0}, job_L[3] = {0, 0, 0};
+    int quad_r = -3, quad_c = 0;
+    if (tid < NMAIN) {
+      const int v = r * C + cc;
+      q0 = __ldg(plane0 + v);
+      q1 = __ldg(plane1 + v);
+      q2 = __ldg(plane2 + v);
+      q3 = __ldg(plane3 + v);
+      if (force_in) F = xyz<float>(force_in[v]) + F;
+      quad_r = lr;
+      quad_c = lc;
+    } else {
+      if (h < TW) {
+        job_kind[0] = KV; job_r[0] = -1; job_c[0] = h;
+        job_kind[1] = KS; job_r[1] = -1; job_c[1] = h;
+        job_kind[2] = KBV; job_r[2] = -1; job_c[2] = h;
+        quad_r = -1; quad_c = h;
+      } else {
+        job_kind[0] = KBV; job_r[0] = -2; job_c[0] = h - TW;
+        if (h < TW + TH) {
+          job_kind[1] = KH; job_r[1] = h - TW; job_c[1] = -1;
+          job_kind[2] = KS; job_r[2] = h - TW; job_c[2] = -1;
+          quad_r = h - TW; quad_c = -1;
+        } else if (h < TW + 2 * TH) {
+          job_kind[1] = KBH; job_r[1] = h - TW - TH; job_c[1] = -2;
+          job_kind[2] = KBH; job_r[2] = h - TW - TH; job_c[2] = -1;
+        } else if (h == TW + 2 * TH) {
+          job_kind[1] = KS; job_r[1] = -1; job_c[1] = -1;
+          quad_r = -1; quad_c = -1;
+        }
+      }
+      const float* pl = reinterpret_cast<const float*>(planes);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (job_kind[j] < 0) continue;
+        const size_t v = size_t((r0 + job_r[j]) * C + c0 + job_c[j]);
+        const int ik = param_index(job_kind[j], 0);
+        job_k[j] = __ldg(pl + size_t(ik >> 2) * 4 * n + 4 * v + (ik & 3));
+        job_cd[j] = __ldg(pl + size_t((ik + 1) >> 2) * 4 * n + 4 * v + ((ik + 1) & 3));
+        job_L[j] = __ldg(pl + size_t((ik + 2) >> 2) * 4 * n + 4 * v + ((ik + 2) & 3));
+      }
+    }
+    __syncthreads();
+
+    // ---- compute every strut and face of the tile once
+    auto put = [&](int kind, int rr, int ccl, float k, float cd, float L) {
+      int ia = e(rr, ccl), ib;
+      switch (kind) {
+        case KH: ib = ia + 1; break;
+        case KV: ib = ia + EW; break;
+        case KS: ib = ia + EW; ia += 1; break;
+        case KBH: ib = ia + 2; break;
+        default: ib = ia + 2 * EW; break;
+      }
+      strut_compact(s_pos, s_vel, ia, ib, k, cd, L, s_su + kind * NO + o(rr, ccl), s_s2 + kind * NO + o(rr, ccl));
+    };
+    if (tid < NMAIN) {
+      put(KH, lr, lc, q0.x, q0.y, q0.z);
+      put(KV, lr, lc, q0.w, q1.x, q1.y);
+      put(KS, lr, lc, q1.z, q1.w, q2.x);
+      put(KBH, lr, lc, q2.y, q2.z, q2.w);
+      put(KBV, lr, lc, q3.x, q3.y, q3.z);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (job_kind[j] >= 0) put(job_kind[j], job_r[j], job_c[j], job_k[j], job_cd[j], job_L[j]);
+    }
+    if (quad_r > -3)
+      quad_to(s_pos, s_vel, e(quad_r, quad_c), e(quad_r, quad_c + 1), e(quad_r + 1, quad_c),
+              e(quad_r + 1, quad_c + 1), wind, c.neg_drag, c.neg_lift, s_qa + qi(quad_r, quad_c),
+              s_qb + qi(quad_r, quad_c), s_qw + qi(quad_r, quad_c));
+    __syncthreads();
+    if (tid >= NMAIN) return;
+
+    // ---- gather in the reference's order for an interior vertex (grid_order.h)
+    auto take = [&](int kind, int rr, int ccl, int role) {
+      const int i = kind * NO + o(rr, ccl);
+      add_compact(F, s_su[i], s_s2[i], role);
+    };
+    take(KS, lr - 1, lc, 1);   // SH_UP
+    take(KV, lr - 1, lc, 1);   // VT_UP
+    take(KS, lr, lc - 1, 0);   // SH_LEFT
+    take(KH, lr, lc - 1, 1);   // HZ_LEFT
+    take(KV, lr, lc, 0);       // VT_DOWN
+    take(KH, lr, lc, 0);       // HZ_RIGHT
+    take(KBV, lr - 2, lc, 1);  // BV_UP
+    take(KBH, lr, lc - 2, 1);  // BH_LEFT
+    take(KBH, lr, lc, 0);      // BH_RIGHT
+    take(KBV, lr, lc, 0);      // BV_DOWN
+    {
+      const int up = qi(lr - 1, lc), left = qi(lr, lc - 1), here = qi(lr, lc), upleft = qi(lr - 1, lc - 1);
+      float4 D = s_qa[up];
+      F = F + s_qw[up].x * V3<float>{D.x, D.y, D.z};  // A_UP, corner 1
+      D = s_qa[left];
+      F = F + D.w * V3<float>{D.x, D.y, D.z};  // A_LEFT, corner 0
+      D = s_qa[here];
+      F = F + s_qw[here].y * V3<float>{D.x, D.y, D.z};  // A_HERE, corner 2
+      D = s_qb[upleft];
+      F = F + s_qw[upleft].z * V3<float>{D.x, D.y, D.z};  // B_UPLEFT, corner 1
+      D = s_qb[up];
+      F = F + s_qw[up].w * V3<float>{D.x, D.y, D.z};  // B_UP, corner 2
+      D = s_qb[left];
+      F = F + D.w * V3<float>{D.x, D.y, D.z};  // B_LEFT, corner 0
+    }
+  } else {
+    // ---- boundary tile: general form with existence checks
+    for (int i = tid; i < G::EH * G::EW; i += NT) {
+      const int gr = r0 - 2 + i / G::EW, gc = c0 - 2 + i % G::EW;
+      if (gr >= 0 && gr < R && gc >= 0 && gc < C) {
+        s_pos[i] = pos[gr * C + gc];
+        s_vel[i] = vel[gr * C + gc];
+      }
+    }
+    __syncthreads();
+    auto sp = [&](int gr, int gc) { return xyz<float>(s_pos[(gr - r0 + 2) * G::EW + (gc - c0 + 2)]); };
+    auto sv = [&](int gr, int gc) { return xyz<float>(s_vel[(gr - r0 + 2) * G::EW + (gc - c0 + 2)]); };
+    auto strut = [&](int kind, int gr, int gc, float4& sf4, float4& df4) {
+      const int ow = gr * C + gc;
+      const float* pl = reinterpret_cast<const float*>(planes);
+      const int ik = param_index(kind, 0);
+      const float k = __ldg(pl + size_t(ik >> 2) * 4 * n + 4 * size_t(ow) + (ik & 3));
+      const float cd = __ldg(pl + size_t((ik + 1) >> 2) * 4 * n + 4 * size_t(ow) + ((ik + 1) & 3));
+      const float L = __ldg(pl + size_t((ik + 2) >> 2) * 4 * n + 4 * size_t(ow) + ((ik + 2) & 3));
+      int ar = gr, ac = gc, br = gr, bc = gc;
+      switch (kind) {
+        case KH: bc = gc + 1; break;
+        case KV: br = gr + 1; break;
+        case KS: ac = gc + 1; br = gr + 1; break;
+        case KBH: bc = gc + 2; break;
+        default: br = gr + 2; break;
+      }
+      V3<float> sf, df;
+      strut_forces<float>(sp(ar, ac), sp(br, bc), sv(ar, ac), sv(br, bc), k, cd, L, sf, df);
+      sf4 = make_float4(sf.x, sf.y, sf.z, 0.0f);
+      df4 = make_float4(df.x, df.y, df.z, 0.0f);
+    };
+    for (int i = tid; i < G::N_TRI; i += NT) {
+      int kind, gr, gc;
+      if (i < G::N_KH) {
+        kind = KH; gr = r0 + i / G::KH_W; gc = c0 - 1 + i % G::KH_W;
+      } else if (i < G::N_KH + G::N_KV) {
+        const int j = i - G::N_KH;
+        kind = KV; gr = r0 - 1 + j / G::KV_W; gc = c0 + j % G::KV_W;
+      } else {
+        const int j = i - G::N_KH - G::N_KV;
+        kind = KS; gr = r0 - 1 + j / G::KS_W; gc = c0 - 1 + j % G::KS_W;
+      }
+      if (owned_exists(kind, gr, gc, R, C)) strut(kind, gr, gc, s_buf[2 * i], s_buf[2 * i + 1]);
+    }
+    __syncthreads();
+    const bool active = tid < NMAIN && r < R && cc < C;
+    if (active && force_in) F = xyz<float>(force_in[r * C + cc]) + F;
+    if (active) {
+      for (int j = 0; j < VT_DOWN + 2; ++j) {  // the six triangle-strut slots
+        const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
+        const int orr = r + d.dr, oc = cc + d.dc;
+        if (!owned_exists(d.kind, orr, oc, R, C)) continue;
+        int idx;
+        if (d.kind == KH) idx = (orr - r0) * G::KH_W + (oc - c0 + 1);
+        else if (d.kind == KV) idx = G::N_KH + (orr - r0 + 1) * G::KV_W + (oc - c0);
+        else idx = G::N_KH + G::N_KV + (orr - r0 + 1) * G::KS_W + (oc - c0 + 1);
+        add_pair(F, s_buf + 2 * idx, d.role);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < G::N_BIND; i += NT) {
+      int kind, gr, gc;
+      if (i < G::N_KBH) {
+        kind = KBH; gr = r0 + i / G::KBH_W; gc = c0 - 2 + i % G::KBH_W;
+      } else {
+        const int j = i - G::N_KBH;
+        kind = KBV; gr = r0 - 2 + j / G::KBV_W; gc = c0 + j % G::KBV_W;
+      }
+      if (owned_exists(kind, gr, gc, R, C)) strut(kind, gr, gc, s_buf[2 * i], s_buf[2 * i + 1]);
+    }
+    __syncthreads();
+    if (active) {
+      for (int j = BV_UP; j < N_SLOTS; ++j) {
+        const SlotDesc d = slot_desc(j);
+        const int orr = r + d.dr, oc = cc + d.dc;
+        if (!owned_exists(d.kind, orr, oc, R, C)) continue;
+        const int idx = d.kind == KBH ? (orr - r0) * G::KBH_W + (oc - c0 + 2)
+                                      : G::N_KBH + (orr - r0 + 2) * G::KBV_W + (oc - c0);
+        add_pair(F, s_buf + 2 * idx, d.role);
+      }
+    }
+    __syncthreads();
+    // quad entry q: s_buf[3q] = A (D, w0), s_buf[3q+1] = B (D, w0), s_buf[3q+2] = (A w1, A w2, B w1, B w2)
+    for (int q = tid; q < G::N_Q; q += NT) {
+      const int qr = r0 - 1 + q / G::Q_W, qc = c0 - 1 + q % G::Q_W;
+      if (!quad_exists(qr, qc, R, C)) continue;
+      const int b00 = (qr - r0 + 2) * G::EW + (qc - c0 + 2);
+      quad_to(s_pos, s_vel, b00, b00 + 1, b00 + G::EW, b00 + G::EW + 1, wind, c.neg_drag, c.neg_lift, s_buf + 3 * q,
+              s_buf + 3 * q + 1, s_buf + 3 * q + 2);
+    }
+    __syncthreads();
+    if (!active) return;
+    for (int s = 0; s < N_FACE_SLOTS; ++s) {
+      const FaceDesc fd = face_desc(s);
+      const int qr = r + fd.dr, qc = cc + fd.dc;
+      if (!quad_exists(qr, qc, R, C)) continue;
+      const int q = (qr - r0 + 1) * G::Q_W + (qc - c0 + 1);
+      const float4 D = s_buf[3 * q + fd.is_b];
+      const float4 W = s_buf[3 * q + 2];
+      float w;
+      if (fd.corner == 0) w = D.w;
+      else if (fd.corner == 1) w = fd.is_b ? W.z : W.x;
+      else w = fd.is_b ? W.w : W.y;
+      F = F + w * V3<float>{D.x, D.y, D.z};
+    }
+  }
+
+  // ---- integrate, collide, write (one thread per tile vertex)
+  const int v = r * C + cc;
+  const float4 P4 = s_pos[(lr + 2) * G::EW + lc + 2];
+  const float4 V4 = s_vel[(lr + 2) * G::EW + lc + 2];
+  if (V4.w != 0.0f) {  // pinned: update_points restores the old point
+    pos_out[v] = P4;
+    vel_out[v] = V4;
+    return;
+  }
+  const V3<float> P = xyz<float>(P4), V = xyz<float>(V4);
+  const float m = P4.w;
+  V3<float> np, nv, nF;
+  integrate_point<float>(c.integration, c.dt, P, V, F, m, np, nv, nF);
+  collide_point<float>(static_cast<const ObsFace*>(c.obstacle_faces), c.n_obstacle_faces, P, V, F, m, np, nv, c);
+  pos_out[v] = make4<float>(np, m);
+  vel_out[v] = make4<float>(nv, V4.w);
+  const bool bad = !(finite3(np) && finite3(nv));
+  if (__any_sync(__activemask(), bad) && bad && c.flags) atomicOr(c.flags, 1u);
+}
+
+constexpr int kTileW = 32, kTileH = 8, kHalo = 64;
+
+size_t tiled_smem_bytes() {
+  using G = TileGeom<kTileW, kTileH>;
+  using I = Interior<kTileW, kTileH>;
+  const size_t staged = 2 * sizeof(float4) * G::EH * G::EW;
+  const size_t boundary = sizeof(float4) * G::BUF;
+  return staged + (size_t(I::BYTES) > boundary ? size_t(I::BYTES) : boundary);
+}
+
 }  // namespace
 
 cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4* vel, const float4* force_in,
                              float4* pos_out, float4* vel_out, const StepConsts& c, cudaStream_t s) {
   const int n = g.rows * g.cols;
   if (n <= 0) return cudaSuccess;
-  k_step_grid_v1<<<(n + 255) / 256, 256, 0, s>>>(g.rows, g.cols, g.params, pos, vel, force_in, pos_out, vel_out, c);
+  if (g.variant == 1) {
+    k_step_grid_v1<<<(n + 255) / 256, 256, 0, s>>>(g.rows, g.cols, g.params, pos, vel, force_in, pos_out, vel_out,
+                                                   c);
+  } else {
+    TileSplit t;
+    t.tx = (g.cols + kTileW - 1) / kTileW;
+    t.ty = (g.rows + kTileH - 1) / kTileH;
+    // interior: c0 >= 2, c0 + TW <= C - 2, r0 >= 2, r0 + TH <= R - 2
+    t.bx0 = 1;
+    t.bx1 = g.cols >= kTileW + 4 ? (g.cols - 2 - kTileW) / kTileW : 0;
+    t.by0 = 1;
+    t.by1 = g.rows >= kTileH + 4 ? (g.rows - 2 - kTileH) / kTileH : 0;
+    const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
+    const int n_interior = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
+    const int n_ring = t.tx * t.ty - n_interior;
+    const size_t smem = tiled_smem_bytes();
+    static bool attr_set = false;  // per process; the attribute is per function on the current device
+    if (!attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    if (n_interior > 0) {
+      const dim3 grid(t.bx1 - t.bx0 + 1, t.by1 - t.by0 + 1);
+      k_step_grid_tiled<kTileW, kTileH, kHalo, true><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
+          g.rows, g.cols, t, g.params, pos, vel, force_in, pos_out, vel_out, c);
+    }
+    if (n_ring > 0)
+      k_step_grid_tiled<kTileW, kTileH, kHalo, false><<<n_ring, kTileW * kTileH + kHalo, smem, s>>>(
+          g.rows, g.cols, t, g.params, pos, vel, force_in, pos_out, vel_out, c);
+  }
   return cudaGetLastError();
 }
 

@@ -136,7 +136,9 @@ int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices);
 
 /* Select the step implementation: 0 = automatic (grid kernel when the mesh
  * is a Cloth::new grid, else the general gather), 1 = general gather,
- * 2 = grid kernel (fails with FGB_ESTATE if the mesh is not a grid). */
+ * 2 = grid kernel (fails with FGB_ESTATE if the mesh is not a grid),
+ * 3 = the grid kernel's untiled form (one thread per vertex, no shared
+ * memory; a cross-check of the tiled one).  All give identical results. */
 int fgb_mesh_set_path(fgb_mesh* m, int path);
 
 /* Which path the next step uses (1 general, 2 grid); decided on the host. */
@@ -188,6 +190,12 @@ int fgb_sim_get_config(const fgb_sim* s, fgb_config* out);
 /* Simulation::step repeated n_steps times -- springy/simulation.rs:27-45.
  * Asynchronous: returns once the launches are queued. */
 int fgb_sim_step(fgb_sim* s, uint64_t n_steps);
+
+/* Collision search: 1 (default) uses an exact broad phase over the obstacle
+ * faces (candidates visited in face order, so the first hit is unchanged);
+ * 0 tests every face for every point like collidable_mesh.rs:107-169.
+ * Extension with no reference counterpart (the results are identical). */
+int fgb_sim_set_collision_broadphase(fgb_sim* s, int enabled);
 
 /* Issue the simulation's work (every mesh) on the caller's CUDA stream
  * (a cudaStream_t passed as void*); NULL returns to the meshes' own streams.
