@@ -179,6 +179,11 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def kernels_per_step(mesh, args):
+    """Launches of this library's kernels per step (every step form is one)."""
+    return 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,7 +340,8 @@ def main():
                            "l2": "flushed (256 MB write) before every timed step",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": args.steps * kernels_per_step(mesh, args),
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
                 "device": torch.cuda.get_device_name()}
         print(json.dumps(line), flush=True)

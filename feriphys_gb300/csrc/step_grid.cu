@@ -255,29 +255,24 @@ __device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, in
 }
 
 template <int TW, int TH, int HALO, bool INTERIOR>
-__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, int C, TileSplit split,
-                                                                      const float4* __restrict__ planes,
-                                                                      const float4* __restrict__ pos,
-                                                                      const float4* __restrict__ vel,
-                                                                      const float4* __restrict__ force_in,
-                                                                      float4* __restrict__ pos_out,
-                                                                      float4* __restrict__ vel_out, StepConsts c) {
+__device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const float4* __restrict__ planes,
+                                          const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                          const float4* __restrict__ force_in, float4* __restrict__ pos_out,
+                                          float4* __restrict__ vel_out, const StepConsts& c) {
   using G = TileGeom<TW, TH>;
   using I = Interior<TW, TH>;
   constexpr int NMAIN = TW * TH, NT = TW * TH + HALO;
-  static_assert(HALO == 2 * TW && TW + TH <= 40 && TW >= 32, "helper layout assumes a 32-wide tile, 64 helpers");
+  static_assert(HALO == 2 * TW && TW + 2 * TH + 1 <= 2 * TW && TW >= 32, "helper layout assumes 64 helpers");
+  constexpr int EW = G::EW, OW = I::OW, NO = I::NO, QW = I::QW, NQ = I::NQ;
   extern __shared__ float4 s_dyn[];
   float4* s_pos = s_dyn;
   float4* s_vel = s_dyn + G::EH * G::EW;
-  float4* s_buf = s_dyn + 2 * G::EH * G::EW;
+  float4* s_su = s_dyn + 2 * G::EH * G::EW;                  // [5][NO] unit vector, s1
+  float* s_s2 = reinterpret_cast<float*>(s_su + 5 * NO);     // [5][NO] s2
+  float4* s_qa = reinterpret_cast<float4*>(s_s2 + 5 * NO);   // [NQ] face A: D, w0
+  float4* s_qb = s_qa + NQ;                                  // [NQ] face B: D, w0
+  float4* s_qw = s_qb + NQ;                                  // [NQ] A w1, A w2, B w1, B w2
   const int n = R * C;
-  int bx, by;
-  if (INTERIOR) {
-    bx = split.bx0 + blockIdx.x;
-    by = split.by0 + blockIdx.y;
-  } else {
-    ring_tile(split, blockIdx.x, bx, by);
-  }
   const int c0 = bx * TW, r0 = by * TH;
   const int tid = threadIdx.x;
   const V3<float> wind{c.wind[0], c.wind[1], c.wind[2]};
@@ -285,117 +280,122 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
   const float4* __restrict__ plane1 = planes + n;
   const float4* __restrict__ plane2 = planes + 2 * size_t(n);
   const float4* __restrict__ plane3 = planes + 3 * size_t(n);
+  auto e = [](int rr, int ccl) { return (rr + 2) * EW + (ccl + 2); };  // tile-relative staged index
+  auto o = [](int rr, int ccl) { return (rr + 2) * OW + (ccl + 2); };  // tile-relative owner index
+  auto qi = [](int rr, int ccl) { return (rr + 1) * QW + (ccl + 1); };
+  // does the strut of `kind` owned by tile-relative (rr, ccl) exist?
+  auto has = [&](int kind, int rr, int ccl) { return INTERIOR || owned_exists(kind, r0 + rr, c0 + ccl, R, C); };
 
-  V3<float> F{c.force0[0], c.force0[1], c.force0[2]};
   const int lr = tid / TW, lc = tid % TW;
   const int r = r0 + lr, cc = c0 + lc;
+  const bool vertex = tid < NMAIN && (INTERIOR || (r < R && cc < C));
+  V3<float> F{c.force0[0], c.force0[1], c.force0[2]};
 
-  if constexpr (INTERIOR) {
-    constexpr int EW = G::EW, OW = I::OW, NO = I::NO, QW = I::QW, NQ = I::NQ;
-    float4* s_su = s_buf;                                      // [5][NO]
-    float* s_s2 = reinterpret_cast<float*>(s_buf + 5 * NO);    // [5][NO]
-    float4* s_qa = reinterpret_cast<float4*>(s_s2 + 5 * NO);   // [NQ]
-    float4* s_qb = s_qa + NQ;
-    float4* s_qw = s_qb + NQ;
-    auto e = [](int rr, int ccl) { return (rr + 2) * EW + (ccl + 2); };  // tile-relative staged index
-    auto o = [](int rr, int ccl) { return (rr + 2) * OW + (ccl + 2); };  // tile-relative owner index
-    auto qi = [](int rr, int ccl) { return (rr + 1) * QW + (ccl + 1); };
-    // ---- stage positions/velocities; prefetch the strut constants this thread needs
-    for (int i = tid; i < G::EH * G::EW; i += NT) {
-      const int g = (r0 - 2 + i / G::EW) * C + (c0 - 2 + i % G::EW);
-      s_pos[i] = pos[g];
-      s_vel[i] = vel[g];
+  // ---- stage positions/velocities; prefetch the strut constants this thread needs
+  for (int i = tid; i < G::EH * G::EW; i += NT) {
+    const int gr = r0 - 2 + i / G::EW, gc = c0 - 2 + i % G::EW;
+    if (INTERIOR || (gr >= 0 && gr < R && gc >= 0 && gc < C)) {
+      s_pos[i] = pos[gr * C + gc];
+      s_vel[i] = vel[gr * C + gc];
     }
-    const int h = tid - NMAIN;
-    // Main threads: the five struts owned by their vertex and its quad.
-    // Helper lanes: up to three strut jobs (kind, owner) and at most one quad,
-    // laid out so a warp never runs two expensive branches one after another:
-    //   h in [0, 32):  owner (-1, h): vertical, shear, vertical binding; quad (-1, h)
-    //   h in [32, 64): vertical binding owned by (-2, h-32), plus
-    //     h in [32, 40): horizontal and shear owned by (h-32, -1); quad (h-32, -1)
-    //     h in [40, 48): horizontal bindings owned by (h-40, -2) and (h-40, -1)
-    //     h == 48:       shear owned by (-1, -1); quad (-1, -1)
-    float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
-    int job_kind[3] = {-1, -1, -1}, job_r[3] = {0, 0, 0}, job_c[3] = {0, 0, 0};
-    float job_k[3] = {0, 0, 0}, job_cd[3] = {0, 0, 0}, job_L[3] = {0, 0, 0};
-    int quad_r = -3, quad_c = 0;
-    if (tid < NMAIN) {
+  }
+  const int h = tid - NMAIN;
+  // Main threads: the five struts owned by their vertex and its quad.
+  // Helper lanes: up to three strut jobs (kind, owner) and at most one quad,
+  // laid out so a warp never runs two expensive branches one after another:
+  //   h in [0, 32):  owner (-1, h): vertical, shear, vertical binding; quad (-1, h)
+  //   h in [32, 64): vertical binding owned by (-2, h-32), plus
+  //     h in [32, 40): horizontal and shear owned by (h-32, -1); quad (h-32, -1)
+  //     h in [40, 48): horizontal bindings owned by (h-40, -2) and (h-40, -1)
+  //     h == 48:       shear owned by (-1, -1); quad (-1, -1)
+  float4 q0 = make_float4(0, 0, 0, 0), q1 = q0, q2 = q0, q3 = q0;
+  int job_kind[3] = {-1, -1, -1}, job_r[3] = {0, 0, 0}, job_c[3] = {0, 0, 0};
+  float job_k[3] = {0, 0, 0}, job_cd[3] = {0, 0, 0}, job_L[3] = {0, 0, 0};
+  int quad_r = -3, quad_c = 0;
+  if (tid < NMAIN) {
+    if (vertex) {
       const int v = r * C + cc;
       q0 = __ldg(plane0 + v);
       q1 = __ldg(plane1 + v);
       q2 = __ldg(plane2 + v);
       q3 = __ldg(plane3 + v);
       if (force_in) F = xyz<float>(force_in[v]) + F;
-      quad_r = lr;
-      quad_c = lc;
+    }
+    quad_r = lr;
+    quad_c = lc;
+  } else {
+    if (h < TW) {
+      job_kind[0] = KV; job_r[0] = -1; job_c[0] = h;
+      job_kind[1] = KS; job_r[1] = -1; job_c[1] = h;
+      job_kind[2] = KBV; job_r[2] = -1; job_c[2] = h;
+      quad_r = -1; quad_c = h;
     } else {
-      if (h < TW) {
-        job_kind[0] = KV; job_r[0] = -1; job_c[0] = h;
-        job_kind[1] = KS; job_r[1] = -1; job_c[1] = h;
-        job_kind[2] = KBV; job_r[2] = -1; job_c[2] = h;
-        quad_r = -1; quad_c = h;
-      } else {
-        job_kind[0] = KBV; job_r[0] = -2; job_c[0] = h - TW;
-        if (h < TW + TH) {
-          job_kind[1] = KH; job_r[1] = h - TW; job_c[1] = -1;
-          job_kind[2] = KS; job_r[2] = h - TW; job_c[2] = -1;
-          quad_r = h - TW; quad_c = -1;
-        } else if (h < TW + 2 * TH) {
-          job_kind[1] = KBH; job_r[1] = h - TW - TH; job_c[1] = -2;
-          job_kind[2] = KBH; job_r[2] = h - TW - TH; job_c[2] = -1;
-        } else if (h == TW + 2 * TH) {
-          job_kind[1] = KS; job_r[1] = -1; job_c[1] = -1;
-          quad_r = -1; quad_c = -1;
-        }
-      }
-      const float* pl = reinterpret_cast<const float*>(planes);
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        if (job_kind[j] < 0) continue;
-        const size_t v = size_t((r0 + job_r[j]) * C + c0 + job_c[j]);
-        const int ik = param_index(job_kind[j], 0);
-        job_k[j] = __ldg(pl + size_t(ik >> 2) * 4 * n + 4 * v + (ik & 3));
-        job_cd[j] = __ldg(pl + size_t((ik + 1) >> 2) * 4 * n + 4 * v + ((ik + 1) & 3));
-        job_L[j] = __ldg(pl + size_t((ik + 2) >> 2) * 4 * n + 4 * v + ((ik + 2) & 3));
+      job_kind[0] = KBV; job_r[0] = -2; job_c[0] = h - TW;
+      if (h < TW + TH) {
+        job_kind[1] = KH; job_r[1] = h - TW; job_c[1] = -1;
+        job_kind[2] = KS; job_r[2] = h - TW; job_c[2] = -1;
+        quad_r = h - TW; quad_c = -1;
+      } else if (h < TW + 2 * TH) {
+        job_kind[1] = KBH; job_r[1] = h - TW - TH; job_c[1] = -2;
+        job_kind[2] = KBH; job_r[2] = h - TW - TH; job_c[2] = -1;
+      } else if (h == TW + 2 * TH) {
+        job_kind[1] = KS; job_r[1] = -1; job_c[1] = -1;
+        quad_r = -1; quad_c = -1;
       }
     }
-    __syncthreads();
-
-    // ---- compute every strut and face of the tile once
-    auto put = [&](int kind, int rr, int ccl, float k, float cd, float L) {
-      int ia = e(rr, ccl), ib;
-      switch (kind) {
-        case KH: ib = ia + 1; break;
-        case KV: ib = ia + EW; break;
-        case KS: ib = ia + EW; ia += 1; break;
-        case KBH: ib = ia + 2; break;
-        default: ib = ia + 2 * EW; break;
-      }
-      strut_compact(s_pos, s_vel, ia, ib, k, cd, L, s_su + kind * NO + o(rr, ccl), s_s2 + kind * NO + o(rr, ccl));
-    };
-    if (tid < NMAIN) {
-      put(KH, lr, lc, q0.x, q0.y, q0.z);
-      put(KV, lr, lc, q0.w, q1.x, q1.y);
-      put(KS, lr, lc, q1.z, q1.w, q2.x);
-      put(KBH, lr, lc, q2.y, q2.z, q2.w);
-      put(KBV, lr, lc, q3.x, q3.y, q3.z);
-    } else {
+    const float* pl = reinterpret_cast<const float*>(planes);
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
-        if (job_kind[j] >= 0) put(job_kind[j], job_r[j], job_c[j], job_k[j], job_cd[j], job_L[j]);
+    for (int j = 0; j < 3; ++j) {
+      if (job_kind[j] < 0 || !has(job_kind[j], job_r[j], job_c[j])) {
+        job_kind[j] = -1;
+        continue;
+      }
+      const size_t v = size_t((r0 + job_r[j]) * C + c0 + job_c[j]);
+      const int ik = param_index(job_kind[j], 0);
+      job_k[j] = __ldg(pl + size_t(ik >> 2) * 4 * n + 4 * v + (ik & 3));
+      job_cd[j] = __ldg(pl + size_t((ik + 1) >> 2) * 4 * n + 4 * v + ((ik + 1) & 3));
+      job_L[j] = __ldg(pl + size_t((ik + 2) >> 2) * 4 * n + 4 * v + ((ik + 2) & 3));
     }
-    if (quad_r > -3)
-      quad_to(s_pos, s_vel, e(quad_r, quad_c), e(quad_r, quad_c + 1), e(quad_r + 1, quad_c),
-              e(quad_r + 1, quad_c + 1), wind, c.neg_drag, c.neg_lift, s_qa + qi(quad_r, quad_c),
-              s_qb + qi(quad_r, quad_c), s_qw + qi(quad_r, quad_c));
-    __syncthreads();
-    if (tid >= NMAIN) return;
+  }
+  if (!INTERIOR && quad_r > -3 && !quad_exists(r0 + quad_r, c0 + quad_c, R, C)) quad_r = -3;
+  __syncthreads();
 
-    // ---- gather in the reference's order for an interior vertex (grid_order.h)
-    auto take = [&](int kind, int rr, int ccl, int role) {
-      const int i = kind * NO + o(rr, ccl);
-      add_compact(F, s_su[i], s_s2[i], role);
-    };
+  // ---- compute every strut and face of the tile once
+  auto put = [&](int kind, int rr, int ccl, float k, float cd, float L) {
+    int ia = e(rr, ccl), ib;
+    switch (kind) {
+      case KH: ib = ia + 1; break;
+      case KV: ib = ia + EW; break;
+      case KS: ib = ia + EW; ia += 1; break;
+      case KBH: ib = ia + 2; break;
+      default: ib = ia + 2 * EW; break;
+    }
+    strut_compact(s_pos, s_vel, ia, ib, k, cd, L, s_su + kind * NO + o(rr, ccl), s_s2 + kind * NO + o(rr, ccl));
+  };
+  if (tid < NMAIN) {
+    if (has(KH, lr, lc)) put(KH, lr, lc, q0.x, q0.y, q0.z);
+    if (has(KV, lr, lc)) put(KV, lr, lc, q0.w, q1.x, q1.y);
+    if (has(KS, lr, lc)) put(KS, lr, lc, q1.z, q1.w, q2.x);
+    if (has(KBH, lr, lc)) put(KBH, lr, lc, q2.y, q2.z, q2.w);
+    if (has(KBV, lr, lc)) put(KBV, lr, lc, q3.x, q3.y, q3.z);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (job_kind[j] >= 0) put(job_kind[j], job_r[j], job_c[j], job_k[j], job_cd[j], job_L[j]);
+  }
+  if (quad_r > -3)
+    quad_to(s_pos, s_vel, e(quad_r, quad_c), e(quad_r, quad_c + 1), e(quad_r + 1, quad_c), e(quad_r + 1, quad_c + 1),
+            wind, c.neg_drag, c.neg_lift, s_qa + qi(quad_r, quad_c), s_qb + qi(quad_r, quad_c),
+            s_qw + qi(quad_r, quad_c));
+  __syncthreads();
+  if (!vertex) return;
+
+  // ---- gather in the reference's summation order (grid_order.h)
+  auto take = [&](int kind, int rr, int ccl, int role) {
+    const int i = kind * NO + o(rr, ccl);
+    add_compact(F, s_su[i], s_s2[i], role);
+  };
+  if (INTERIOR) {
     take(KS, lr - 1, lc, 1);   // SH_UP
     take(KV, lr - 1, lc, 1);   // VT_UP
     take(KS, lr, lc - 1, 0);   // SH_LEFT
@@ -406,133 +406,28 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
     take(KBH, lr, lc - 2, 1);  // BH_LEFT
     take(KBH, lr, lc, 0);      // BH_RIGHT
     take(KBV, lr, lc, 0);      // BV_DOWN
-    {
-      const int up = qi(lr - 1, lc), left = qi(lr, lc - 1), here = qi(lr, lc), upleft = qi(lr - 1, lc - 1);
-      float4 D = s_qa[up];
-      F = F + s_qw[up].x * V3<float>{D.x, D.y, D.z};  // A_UP, corner 1
-      D = s_qa[left];
-      F = F + D.w * V3<float>{D.x, D.y, D.z};  // A_LEFT, corner 0
-      D = s_qa[here];
-      F = F + s_qw[here].y * V3<float>{D.x, D.y, D.z};  // A_HERE, corner 2
-      D = s_qb[upleft];
-      F = F + s_qw[upleft].z * V3<float>{D.x, D.y, D.z};  // B_UPLEFT, corner 1
-      D = s_qb[up];
-      F = F + s_qw[up].w * V3<float>{D.x, D.y, D.z};  // B_UP, corner 2
-      D = s_qb[left];
-      F = F + D.w * V3<float>{D.x, D.y, D.z};  // B_LEFT, corner 0
-    }
   } else {
-    // ---- boundary tile: general form with existence checks
-    for (int i = tid; i < G::EH * G::EW; i += NT) {
-      const int gr = r0 - 2 + i / G::EW, gc = c0 - 2 + i % G::EW;
-      if (gr >= 0 && gr < R && gc >= 0 && gc < C) {
-        s_pos[i] = pos[gr * C + gc];
-        s_vel[i] = vel[gr * C + gc];
-      }
-    }
-    __syncthreads();
-    auto sp = [&](int gr, int gc) { return xyz<float>(s_pos[(gr - r0 + 2) * G::EW + (gc - c0 + 2)]); };
-    auto sv = [&](int gr, int gc) { return xyz<float>(s_vel[(gr - r0 + 2) * G::EW + (gc - c0 + 2)]); };
-    auto strut = [&](int kind, int gr, int gc, float4& sf4, float4& df4) {
-      const int ow = gr * C + gc;
-      const float* pl = reinterpret_cast<const float*>(planes);
-      const int ik = param_index(kind, 0);
-      const float k = __ldg(pl + size_t(ik >> 2) * 4 * n + 4 * size_t(ow) + (ik & 3));
-      const float cd = __ldg(pl + size_t((ik + 1) >> 2) * 4 * n + 4 * size_t(ow) + ((ik + 1) & 3));
-      const float L = __ldg(pl + size_t((ik + 2) >> 2) * 4 * n + 4 * size_t(ow) + ((ik + 2) & 3));
-      int ar = gr, ac = gc, br = gr, bc = gc;
-      switch (kind) {
-        case KH: bc = gc + 1; break;
-        case KV: br = gr + 1; break;
-        case KS: ac = gc + 1; br = gr + 1; break;
-        case KBH: bc = gc + 2; break;
-        default: br = gr + 2; break;
-      }
-      V3<float> sf, df;
-      strut_forces<float>(sp(ar, ac), sp(br, bc), sv(ar, ac), sv(br, bc), k, cd, L, sf, df);
-      sf4 = make_float4(sf.x, sf.y, sf.z, 0.0f);
-      df4 = make_float4(df.x, df.y, df.z, 0.0f);
-    };
-    for (int i = tid; i < G::N_TRI; i += NT) {
-      int kind, gr, gc;
-      if (i < G::N_KH) {
-        kind = KH; gr = r0 + i / G::KH_W; gc = c0 - 1 + i % G::KH_W;
-      } else if (i < G::N_KH + G::N_KV) {
-        const int j = i - G::N_KH;
-        kind = KV; gr = r0 - 1 + j / G::KV_W; gc = c0 + j % G::KV_W;
-      } else {
-        const int j = i - G::N_KH - G::N_KV;
-        kind = KS; gr = r0 - 1 + j / G::KS_W; gc = c0 - 1 + j % G::KS_W;
-      }
-      if (owned_exists(kind, gr, gc, R, C)) strut(kind, gr, gc, s_buf[2 * i], s_buf[2 * i + 1]);
-    }
-    __syncthreads();
-    const bool active = tid < NMAIN && r < R && cc < C;
-    if (active && force_in) F = xyz<float>(force_in[r * C + cc]) + F;
-    if (active) {
-      for (int j = 0; j < VT_DOWN + 2; ++j) {  // the six triangle-strut slots
-        const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
-        const int orr = r + d.dr, oc = cc + d.dc;
-        if (!owned_exists(d.kind, orr, oc, R, C)) continue;
-        int idx;
-        if (d.kind == KH) idx = (orr - r0) * G::KH_W + (oc - c0 + 1);
-        else if (d.kind == KV) idx = G::N_KH + (orr - r0 + 1) * G::KV_W + (oc - c0);
-        else idx = G::N_KH + G::N_KV + (orr - r0 + 1) * G::KS_W + (oc - c0 + 1);
-        add_pair(F, s_buf + 2 * idx, d.role);
-      }
-    }
-    __syncthreads();
-    for (int i = tid; i < G::N_BIND; i += NT) {
-      int kind, gr, gc;
-      if (i < G::N_KBH) {
-        kind = KBH; gr = r0 + i / G::KBH_W; gc = c0 - 2 + i % G::KBH_W;
-      } else {
-        const int j = i - G::N_KBH;
-        kind = KBV; gr = r0 - 2 + j / G::KBV_W; gc = c0 + j % G::KBV_W;
-      }
-      if (owned_exists(kind, gr, gc, R, C)) strut(kind, gr, gc, s_buf[2 * i], s_buf[2 * i + 1]);
-    }
-    __syncthreads();
-    if (active) {
-      for (int j = BV_UP; j < N_SLOTS; ++j) {
-        const SlotDesc d = slot_desc(j);
-        const int orr = r + d.dr, oc = cc + d.dc;
-        if (!owned_exists(d.kind, orr, oc, R, C)) continue;
-        const int idx = d.kind == KBH ? (orr - r0) * G::KBH_W + (oc - c0 + 2)
-                                      : G::N_KBH + (orr - r0 + 2) * G::KBV_W + (oc - c0);
-        add_pair(F, s_buf + 2 * idx, d.role);
-      }
-    }
-    __syncthreads();
-    // quad entry q: s_buf[3q] = A (D, w0), s_buf[3q+1] = B (D, w0), s_buf[3q+2] = (A w1, A w2, B w1, B w2)
-    for (int q = tid; q < G::N_Q; q += NT) {
-      const int qr = r0 - 1 + q / G::Q_W, qc = c0 - 1 + q % G::Q_W;
-      if (!quad_exists(qr, qc, R, C)) continue;
-      const int b00 = (qr - r0 + 2) * G::EW + (qc - c0 + 2);
-      quad_to(s_pos, s_vel, b00, b00 + 1, b00 + G::EW, b00 + G::EW + 1, wind, c.neg_drag, c.neg_lift, s_buf + 3 * q,
-              s_buf + 3 * q + 1, s_buf + 3 * q + 2);
-    }
-    __syncthreads();
-    if (!active) return;
-    for (int s = 0; s < N_FACE_SLOTS; ++s) {
-      const FaceDesc fd = face_desc(s);
-      const int qr = r + fd.dr, qc = cc + fd.dc;
-      if (!quad_exists(qr, qc, R, C)) continue;
-      const int q = (qr - r0 + 1) * G::Q_W + (qc - c0 + 1);
-      const float4 D = s_buf[3 * q + fd.is_b];
-      const float4 W = s_buf[3 * q + 2];
-      float w;
-      if (fd.corner == 0) w = D.w;
-      else if (fd.corner == 1) w = fd.is_b ? W.z : W.x;
-      else w = fd.is_b ? W.w : W.y;
-      F = F + w * V3<float>{D.x, D.y, D.z};
+    for (int j = 0; j < N_SLOTS; ++j) {
+      const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
+      if (owned_exists(d.kind, r + d.dr, cc + d.dc, R, C)) take(d.kind, lr + d.dr, lc + d.dc, d.role);
     }
   }
+  for (int sl = 0; sl < N_FACE_SLOTS; ++sl) {
+    const FaceDesc fd = face_desc(sl);
+    if (!INTERIOR && !quad_exists(r + fd.dr, cc + fd.dc, R, C)) continue;
+    const int q = qi(lr + fd.dr, lc + fd.dc);
+    const float4 D = fd.is_b ? s_qb[q] : s_qa[q];
+    float w;
+    if (fd.corner == 0) w = D.w;
+    else if (fd.corner == 1) w = fd.is_b ? s_qw[q].z : s_qw[q].x;
+    else w = fd.is_b ? s_qw[q].w : s_qw[q].y;
+    F = F + w * V3<float>{D.x, D.y, D.z};
+  }
 
-  // ---- integrate, collide, write (one thread per tile vertex)
+  // ---- integrate, collide, write
   const int v = r * C + cc;
-  const float4 P4 = s_pos[(lr + 2) * G::EW + lc + 2];
-  const float4 V4 = s_vel[(lr + 2) * G::EW + lc + 2];
+  const float4 P4 = s_pos[e(lr, lc)];
+  const float4 V4 = s_vel[e(lr, lc)];
   if (V4.w != 0.0f) {  // pinned: update_points restores the old point
     pos_out[v] = P4;
     vel_out[v] = V4;
@@ -549,14 +444,34 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
   if (__any_sync(__activemask(), bad) && bad && c.flags) atomicOr(c.flags, 1u);
 }
 
+// One launch for all tiles: the boundary ring first (its tiles are slower
+// and then overlap the interior ones instead of running as a lone wave).
+template <int TW, int TH, int HALO>
+__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, int C, TileSplit split, int n_ring,
+                                                                      const float4* __restrict__ planes,
+                                                                      const float4* __restrict__ pos,
+                                                                      const float4* __restrict__ vel,
+                                                                      const float4* __restrict__ force_in,
+                                                                      float4* __restrict__ pos_out,
+                                                                      float4* __restrict__ vel_out, StepConsts c) {
+  const int b = blockIdx.x;
+  if (b < n_ring) {
+    int bx, by;
+    ring_tile(split, b, bx, by);
+    tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c);
+  } else {
+    const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
+    tile_step<TW, TH, HALO, true>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel, force_in,
+                                  pos_out, vel_out, c);
+  }
+}
+
 constexpr int kTileW = 32, kTileH = 8, kHalo = 64;
 
 size_t tiled_smem_bytes() {
   using G = TileGeom<kTileW, kTileH>;
   using I = Interior<kTileW, kTileH>;
-  const size_t staged = 2 * sizeof(float4) * G::EH * G::EW;
-  const size_t boundary = sizeof(float4) * G::BUF;
-  return staged + (size_t(I::BYTES) > boundary ? size_t(I::BYTES) : boundary);
+  return 2 * sizeof(float4) * G::EH * G::EW + size_t(I::BYTES);
 }
 
 }  // namespace
@@ -583,22 +498,13 @@ cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4*
     const size_t smem = tiled_smem_bytes();
     static bool attr_set = false;  // per process; the attribute is per function on the current device
     if (!attr_set) {
-      cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      const cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
-    if (n_interior > 0) {
-      const dim3 grid(t.bx1 - t.bx0 + 1, t.by1 - t.by0 + 1);
-      k_step_grid_tiled<kTileW, kTileH, kHalo, true><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
-          g.rows, g.cols, t, g.params, pos, vel, force_in, pos_out, vel_out, c);
-    }
-    if (n_ring > 0)
-      k_step_grid_tiled<kTileW, kTileH, kHalo, false><<<n_ring, kTileW * kTileH + kHalo, smem, s>>>(
-          g.rows, g.cols, t, g.params, pos, vel, force_in, pos_out, vel_out, c);
+    k_step_grid_tiled<kTileW, kTileH, kHalo><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
+        g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c);
   }
   return cudaGetLastError();
 }
