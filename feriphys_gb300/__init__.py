@@ -130,6 +130,10 @@ def _declare(l):
         "fgb_sim_step": (I, [P, U64]),
         "fgb_sim_set_stream": (I, [P, P]),
         "fgb_sim_set_collision_broadphase": (I, [P, I]),
+        "fgb_mesh_set_wind": (I, [P, P]),
+        "fgb_sim_set_graphs": (I, [P, I]),
+        "fgb_sim_set_batch_mode": (I, [P, I]),
+        "fgb_sim_batch_info": (I, [P, P]),
         "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
         "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
         "fgb_sim_destroy": (I, [P]),
@@ -301,6 +305,14 @@ class SpringyMesh:
         _check(_lib().fgb_mesh_get_path(self._h, C.byref(p)))
         return p.value
 
+    def set_wind(self, wind):
+        """Per-mesh wind (extension); None returns to the simulation's wind."""
+        if wind is None:
+            _check(_lib().fgb_mesh_set_wind(self._h, None))
+        else:
+            w = _f32(wind)
+            _check(_lib().fgb_mesh_set_wind(self._h, _ptr(w)))
+
     def set_precision(self, bits: int):
         _check(_lib().fgb_mesh_set_precision(self._h, int(bits)))
 
@@ -411,6 +423,19 @@ class Simulation:
         simulated seconds of one step like the reference's Duration."""
         _check(_lib().fgb_sim_step(self._h, int(n_steps)))
         return self.get_timestep()
+
+    def set_batch_mode(self, mode: int):
+        """-1 autotuned (default), 0 one CTA per tile, 1 persistent."""
+        _check(_lib().fgb_sim_set_batch_mode(self._h, int(mode)))
+
+    def set_graphs(self, enabled: bool):
+        _check(_lib().fgb_sim_set_graphs(self._h, 1 if enabled else 0))
+
+    def batch_info(self):
+        """(meshes in the batch, work items, launch form, persistent CTAs)."""
+        out = np.zeros(4, np.int64)
+        _check(_lib().fgb_sim_batch_info(self._h, _ptr(out)))
+        return tuple(int(v) for v in out)
 
     def set_collision_broadphase(self, enabled: bool):
         """True (default): exact broad phase; False: test every obstacle face."""

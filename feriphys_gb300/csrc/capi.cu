@@ -1,14 +1,20 @@
 // C ABI implementation (include/feriphys_gb300.h): handles, device memory,
 // streams and kernel launches.  Host-side construction lives in
 // mesh_build.cpp; the kernels in step_general.cu / step_grid.cu / state_io.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <new>
 #include <set>
 #include <string>
 #include <utility>
 #include <vector>
+
+#include <sys/stat.h>
 
 #include "feriphys_gb300.h"
 #include "kernels.h"
@@ -60,6 +66,15 @@ bool finite_nonneg(float x) { return std::isfinite(x) && x >= 0.0f; }
 
 }  // namespace
 
+// A library-created stream shared by every mesh that issues work on it (all
+// meshes of a batched simulation share one); destroyed with its last user.
+struct StreamOwner {
+  cudaStream_t s = nullptr;
+  ~StreamOwner() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
 struct fgb_obstacle {
   uint64_t n_vertices = 0;
   uint64_t n_edges = 0;
@@ -74,8 +89,10 @@ struct fgb_mesh {
   int precision = 32;    // 32 or 64
   int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
   cudaStream_t stream = nullptr;      // the stream all work of this mesh is issued on
-  cudaStream_t own_stream = nullptr;  // created by the library (destroyed with the mesh)
+  std::shared_ptr<StreamOwner> own;   // library stream (possibly shared with a batch)
   bool external_stream = false;
+  float wind[3] = {0, 0, 0};          // per-mesh wind (extension), used when has_wind
+  bool has_wind = false;
 
   // host copy of the state while the device does not hold it (as_state layout)
   std::vector<float> host_pts;
@@ -123,6 +140,22 @@ struct fgb_sim {
   bool broadphase = true;
   fgb::ObsAccel accel{};  // device broad phase (pointers into d_accel)
   int* d_accel = nullptr;
+  // batched stepping of grid meshes (two or more): one kernel per step
+  std::vector<fgb_mesh*> batch;           // grid meshes, largest first
+  std::vector<fgb::ClothDesc> desc;       // host copy of the device table
+  fgb::ClothDesc* d_desc = nullptr;
+  size_t d_desc_cap = 0;
+  int4* d_work = nullptr;
+  int n_work = 0;
+  int* d_counter = nullptr;
+  int parity = 0;
+  int mode = -1, ctas = 0;                // launch form chosen by the tuner
+  int forced_mode = -1;                   // fgb_sim_set_batch_mode (-1: tuner)
+  bool graphs = true;
+  std::map<std::pair<uint64_t, int>, cudaGraphExec_t> graph_cache;
+  fgb_config graph_cfg;
+  std::shared_ptr<StreamOwner> stream;    // shared with the batch's meshes
+  cudaStream_t ext_stream = nullptr;      // caller's stream (fgb_sim_set_stream), if any
 };
 
 namespace {
@@ -141,8 +174,11 @@ void init_host_state(fgb_mesh* m) {
 }
 
 int ensure_stream(fgb_mesh* m) {
-  if (!m->own_stream) FGB_CUDA(cudaStreamCreateWithFlags(&m->own_stream, cudaStreamNonBlocking));
-  if (!m->external_stream) m->stream = m->own_stream;
+  if (!m->own) {
+    m->own = std::make_shared<StreamOwner>();
+    FGB_CUDA(cudaStreamCreateWithFlags(&m->own->s, cudaStreamNonBlocking));
+  }
+  if (!m->external_stream) m->stream = m->own->s;
   return FGB_OK;
 }
 
@@ -373,6 +409,238 @@ int step_mesh(fgb_mesh* m, const fgb::StepConsts& c) {
   m->cur = nxt;
   m->has_force = false;  // clear_forces
   m->staged = false;
+  return FGB_OK;
+}
+
+cudaStream_t batch_stream(const fgb_sim* s) { return s->ext_stream ? s->ext_stream : s->stream->s; }
+
+void drop_graphs(fgb_sim* s) {
+  for (auto& kv : s->graph_cache) cudaGraphExecDestroy(kv.second);
+  s->graph_cache.clear();
+}
+
+// Grid meshes stepped together (two or more): largest first, one shared
+// stream, buffers aligned to the simulation's parity, descriptor table and
+// work list uploaded when they change.
+int prepare_batch(fgb_sim* s) {
+  std::vector<fgb_mesh*> grid;
+  for (fgb_mesh* m : s->meshes)
+    if (m->active_path == 2 && m->grid_variant == 0 && m->precision == 32) grid.push_back(m);
+  if (grid.size() < 2) {
+    s->batch.clear();
+    return FGB_OK;
+  }
+  std::stable_sort(grid.begin(), grid.end(), [](const fgb_mesh* a, const fgb_mesh* b) { return a->topo.n > b->topo.n; });
+  if (!s->stream) s->stream = grid[0]->own;
+  const cudaStream_t bs = batch_stream(s);
+  for (fgb_mesh* m : grid) {
+    if (m->stream != bs) {
+      if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
+      if (s->ext_stream) {
+        m->external_stream = true;
+      } else {
+        m->own = s->stream;
+        m->external_stream = false;
+      }
+      m->stream = bs;
+    }
+    if (m->cur != s->parity) {
+      std::swap(m->pos[0], m->pos[1]);
+      std::swap(m->vel[0], m->vel[1]);
+      m->cur = s->parity;
+    }
+  }
+  const bool membership = grid != s->batch;
+  std::vector<fgb::ClothDesc> desc(grid.size());
+  for (size_t i = 0; i < grid.size(); ++i) {
+    fgb_mesh* m = grid[i];
+    fgb::ClothDesc& d = desc[i];
+    std::memset(&d, 0, sizeof(d));
+    d.planes = m->d_grid;
+    for (int k = 0; k < 2; ++k) {
+      d.pos[k] = static_cast<float4*>(m->pos[k]);
+      d.vel[k] = static_cast<float4*>(m->vel[k]);
+    }
+    d.force_in = m->has_force ? static_cast<const float4*>(m->force) : nullptr;
+    d.flags = m->d_flags;
+    d.rows = int(m->topo.rows);
+    d.cols = int(m->topo.cols);
+    for (int k = 0; k < 3; ++k) d.wind[k] = m->has_wind ? m->wind[k] : s->cfg.wind[k];
+  }
+  if (membership) {
+    std::vector<int> work;
+    for (size_t i = 0; i < grid.size(); ++i) {
+      int nr, ni;
+      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), nullptr, &nr, &ni);
+      const size_t at = work.size();
+      work.resize(at + 4 * size_t(nr + ni));
+      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), work.data() + at, &nr, &ni);
+    }
+    s->n_work = int(work.size() / 4);
+    FGB_CUDA(dalloc(s->d_work, work.size() * sizeof(int)));
+    FGB_CUDA(cudaMemcpy(s->d_work, work.data(), work.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!s->d_counter) FGB_CUDA(dalloc(s->d_counter, sizeof(int)));
+    drop_graphs(s);
+    s->mode = -1;
+  }
+  if (membership || desc.size() != s->desc.size() ||
+      std::memcmp(desc.data(), s->desc.data(), desc.size() * sizeof(fgb::ClothDesc)) != 0) {
+    if (s->d_desc_cap < desc.size()) {
+      FGB_CUDA(dalloc(s->d_desc, desc.size() * sizeof(fgb::ClothDesc)));
+      s->d_desc_cap = desc.size();
+      drop_graphs(s);
+    }
+    FGB_CUDA(cudaMemcpyAsync(s->d_desc, desc.data(), desc.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice,
+                             bs));
+    FGB_CUDA(cudaStreamSynchronize(bs));
+    s->desc = std::move(desc);
+  }
+  s->batch = std::move(grid);
+  return FGB_OK;
+}
+
+int batch_launch(fgb_sim* s, int parity, int mode, int ctas) {
+  cudaStream_t st = batch_stream(s);
+  FGB_CUDA(cudaMemsetAsync(s->d_counter, 0, sizeof(int), st));
+  FGB_CUDA(fgb::launch_step_batched(s->d_desc, s->d_work, s->n_work, s->d_counter, parity, mode, ctas,
+                                    make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st));
+  return FGB_OK;
+}
+
+// Autotuner: times the launch forms on this batch (launches that read the
+// current buffers and write the other ones, so the state is untouched) and
+// caches the winner per GPU and batch size in a text file
+// ($FGB_AUTOTUNE_CACHE, default ~/.cache/feriphys_gb300/autotune.txt).
+std::string tune_cache_path() {
+  if (const char* p = std::getenv("FGB_AUTOTUNE_CACHE")) return p;
+  const char* home = std::getenv("HOME");
+  return std::string(home ? home : "/tmp") + "/.cache/feriphys_gb300/autotune.txt";
+}
+
+int tune_batch(fgb_sim* s) {
+  if (s->forced_mode >= 0) {
+    s->mode = s->forced_mode;
+    int dev = 0, sms = 0;
+    FGB_CUDA(cudaGetDevice(&dev));
+    FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    s->ctas = fgb::batched_ctas_per_sm() * sms;
+    return FGB_OK;
+  }
+  int dev = 0;
+  FGB_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  FGB_CUDA(cudaGetDeviceProperties(&prop, dev));
+  int bucket = 0;
+  while ((1 << bucket) < s->n_work) ++bucket;
+  char key[512];
+  std::snprintf(key, sizeof(key), "batched %s sms=%d work=2^%d", prop.name, prop.multiProcessorCount, bucket);
+  for (char* c = key; *c; ++c)
+    if (*c == '\n') *c = ' ';
+  const std::string path = tune_cache_path();
+  if (FILE* f = std::fopen(path.c_str(), "r")) {
+    char line[600];
+    while (std::fgets(line, sizeof(line), f)) {
+      int mode = -1, per_sm = 0;
+      const char* sep = std::strstr(line, " -> ");
+      if (!sep || std::string(line, sep - line) != key) continue;
+      if (std::sscanf(sep + 4, "mode=%d ctas_per_sm=%d", &mode, &per_sm) == 2 && (mode == 0 || mode == 1)) {
+        s->mode = mode;
+        s->ctas = per_sm * prop.multiProcessorCount;
+      }
+    }
+    std::fclose(f);
+    if (s->mode >= 0) return FGB_OK;
+  }
+  const int per_sm = fgb::batched_ctas_per_sm();
+  const int cand_mode[2] = {0, 1};
+  float best = 1e30f;
+  int best_mode = 0;
+  cudaEvent_t a, b;
+  FGB_CUDA(cudaEventCreate(&a));
+  FGB_CUDA(cudaEventCreate(&b));
+  for (int ci = 0; ci < 2; ++ci) {
+    const int ctas = per_sm * prop.multiProcessorCount;
+    FGB_CHECK_RC(batch_launch(s, s->parity, cand_mode[ci], ctas));  // warm-up
+    FGB_CUDA(cudaEventRecord(a, batch_stream(s)));
+    for (int r = 0; r < 5; ++r) FGB_CHECK_RC(batch_launch(s, s->parity, cand_mode[ci], ctas));
+    FGB_CUDA(cudaEventRecord(b, batch_stream(s)));
+    FGB_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    FGB_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (ms < best) {
+      best = ms;
+      best_mode = cand_mode[ci];
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  s->mode = best_mode;
+  s->ctas = per_sm * prop.multiProcessorCount;
+  const std::string dir = path.substr(0, path.rfind('/'));
+  std::string cmd_dir = dir;
+  // create the cache directory (best effort) and append the result
+  for (size_t i = 1; i <= cmd_dir.size(); ++i)
+    if (i == cmd_dir.size() || cmd_dir[i] == '/') {
+      const std::string sub = cmd_dir.substr(0, i);
+      mkdir(sub.c_str(), 0755);
+    }
+  if (FILE* f = std::fopen(path.c_str(), "a")) {
+    std::fprintf(f, "%s -> mode=%d ctas_per_sm=%d time_ms=%.4f\n", key, best_mode, per_sm, best / 5.0f);
+    std::fclose(f);
+  }
+  return FGB_OK;
+}
+
+int batched_steps(fgb_sim* s, uint64_t n) {
+  cudaStream_t st = batch_stream(s);
+  if (n == 0) return FGB_OK;
+  bool forces = false;
+  for (fgb_mesh* m : s->batch) forces = forces || m->has_force;
+  if (forces) {  // the first step carries accumulated forces: run it directly
+    if (s->mode < 0) FGB_CHECK_RC(tune_batch(s));
+    FGB_CHECK_RC(batch_launch(s, s->parity, s->mode, s->ctas));
+    s->parity ^= 1;
+    for (fgb_mesh* m : s->batch) {
+      m->cur = s->parity;
+      m->has_force = false;
+      m->staged = false;
+    }
+    FGB_CHECK_RC(prepare_batch(s));
+    --n;
+    if (n == 0) return FGB_OK;
+  }
+  if (s->mode < 0) FGB_CHECK_RC(tune_batch(s));
+  if (std::memcmp(&s->graph_cfg, &s->cfg, sizeof(fgb_config)) != 0) {
+    drop_graphs(s);
+    s->graph_cfg = s->cfg;
+  }
+  if (s->graphs && n >= 2) {
+    const auto key = std::make_pair(uint64_t(n), s->parity | (s->accel.enabled << 1));
+    auto it = s->graph_cache.find(key);
+    if (it == s->graph_cache.end()) {
+      cudaGraph_t g;
+      FGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      int rc = FGB_OK;
+      for (uint64_t k = 0; k < n && rc == FGB_OK; ++k) rc = batch_launch(s, s->parity ^ int(k & 1), s->mode, s->ctas);
+      const cudaError_t e = cudaStreamEndCapture(st, &g);
+      if (rc != FGB_OK) return rc;
+      FGB_CUDA(e);
+      cudaGraphExec_t exec;
+      const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      FGB_CUDA(ei);
+      it = s->graph_cache.emplace(key, exec).first;
+    }
+    FGB_CUDA(cudaGraphLaunch(it->second, st));
+  } else {
+    for (uint64_t k = 0; k < n; ++k) FGB_CHECK_RC(batch_launch(s, s->parity ^ int(k & 1), s->mode, s->ctas));
+  }
+  s->parity ^= int(n & 1);
+  for (fgb_mesh* m : s->batch) {
+    m->cur = s->parity;
+    m->has_force = false;
+    m->staged = false;
+  }
   return FGB_OK;
 }
 
@@ -729,7 +997,7 @@ int fgb_mesh_destroy(fgb_mesh* m) {
   dfree(m->d_io);
   dfree(m->d_pinned);
   dfree(m->d_flags);
-  if (m->own_stream) cudaStreamDestroy(m->own_stream);
+  m->own.reset();
   delete m;
   return FGB_OK;
 }
@@ -863,9 +1131,47 @@ int fgb_sim_step(fgb_sim* s, uint64_t n_steps) {
   }
   s->accel.enabled = (s->broadphase && s->d_accel) ? 1 : 0;
   for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_device(m));
+  FGB_CHECK_RC(prepare_batch(s));
+  if (!s->batch.empty()) FGB_CHECK_RC(batched_steps(s, n_steps));
+  std::set<fgb_mesh*> in_batch(s->batch.begin(), s->batch.end());
   for (uint64_t k = 0; k < n_steps; ++k)
     for (fgb_mesh* m : s->meshes)
-      FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags, &s->accel)));
+      if (!in_batch.count(m))
+        FGB_CHECK_RC(step_mesh(m, make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags, &s->accel)));
+  return FGB_OK;
+}
+
+int fgb_mesh_set_wind(fgb_mesh* m, const float* wind) {
+  if (!m) return fail(FGB_EINVAL, "null mesh");
+  if (wind) {
+    for (int k = 0; k < 3; ++k) m->wind[k] = wind[k];
+    m->has_wind = true;
+  } else {
+    m->has_wind = false;
+  }
+  return FGB_OK;
+}
+
+int fgb_sim_set_batch_mode(fgb_sim* s, int mode) {
+  if (!s || mode < -1 || mode > 1) return fail(FGB_EINVAL, "mode must be -1, 0 or 1");
+  s->forced_mode = mode;
+  s->mode = -1;
+  drop_graphs(s);
+  return FGB_OK;
+}
+
+int fgb_sim_set_graphs(fgb_sim* s, int enabled) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  s->graphs = enabled != 0;
+  return FGB_OK;
+}
+
+int fgb_sim_batch_info(const fgb_sim* s, int64_t out[4]) {
+  if (!s || !out) return fail(FGB_EINVAL, "null argument");
+  out[0] = int64_t(s->batch.size());
+  out[1] = s->n_work;
+  out[2] = s->mode;
+  out[3] = s->ctas;
   return FGB_OK;
 }
 
@@ -877,10 +1183,11 @@ int fgb_sim_set_collision_broadphase(fgb_sim* s, int enabled) {
 
 int fgb_sim_set_stream(fgb_sim* s, void* stream) {
   if (!s) return fail(FGB_EINVAL, "null sim");
+  s->ext_stream = static_cast<cudaStream_t>(stream);
   for (fgb_mesh* m : s->meshes) {
     if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
     m->external_stream = stream != nullptr;
-    m->stream = stream ? static_cast<cudaStream_t>(stream) : m->own_stream;
+    m->stream = stream ? static_cast<cudaStream_t>(stream) : (m->own ? m->own->s : nullptr);
   }
   return FGB_OK;
 }
@@ -916,6 +1223,10 @@ int fgb_sim_destroy(fgb_sim* s) {
   // for in-flight work that reads the obstacle faces.
   dfree(s->d_faces);
   dfree(s->d_accel);
+  for (auto& kv : s->graph_cache) cudaGraphExecDestroy(kv.second);
+  dfree(s->d_desc);
+  dfree(s->d_work);
+  dfree(s->d_counter);
   delete s;
   return FGB_OK;
 }

@@ -45,4 +45,26 @@ cudaError_t launch_zero4(int n, void* a, cudaStream_t s);
 cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4* vel, const float4* force_in,
                              float4* pos_out, float4* vel_out, const StepConsts& c, cudaStream_t s);
 
+// One cloth of a batch (Cloth::new topology); buffers [parity] are read and
+// [parity ^ 1] written by a step.
+struct ClothDesc {
+  const float4* planes;
+  float4* pos[2];
+  float4* vel[2];
+  const float4* force_in;  // accumulated force carried into the step, or null
+  unsigned* flags;         // non-finite flag of this cloth
+  int rows, cols;
+  float wind[3];
+  int pad;
+};
+
+// Tiles of one cloth for the batch work list: {cloth, tile x, tile y, interior}.
+void batch_tiles(int cloth, int rows, int cols, int* out4 /* may be null */, int* n_ring, int* n_interior);
+
+// mode 0: one CTA per work item; mode 1: persistent CTAs pulling items from
+// *counter (reset to 0 by the caller before the launch).
+cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
+                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s);
+int batched_ctas_per_sm();
+
 }  // namespace fgb

@@ -254,11 +254,14 @@ __device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, in
   bx = j < t.bx0 ? j : t.bx1 + 1 + (j - t.bx0);
 }
 
+// One tile of one cloth.  No early return: the batched kernel runs it in a
+// loop, so every thread reaches the end of every tile.
 template <int TW, int TH, int HALO, bool INTERIOR>
 __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const float4* __restrict__ planes,
                                           const float4* __restrict__ pos, const float4* __restrict__ vel,
                                           const float4* __restrict__ force_in, float4* __restrict__ pos_out,
-                                          float4* __restrict__ vel_out, const StepConsts& c) {
+                                          float4* __restrict__ vel_out, const StepConsts& c, V3<float> wind,
+                                          unsigned* flags) {
   using G = TileGeom<TW, TH>;
   using I = Interior<TW, TH>;
   constexpr int NMAIN = TW * TH, NT = TW * TH + HALO;
@@ -275,7 +278,6 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   const int n = R * C;
   const int c0 = bx * TW, r0 = by * TH;
   const int tid = threadIdx.x;
-  const V3<float> wind{c.wind[0], c.wind[1], c.wind[2]};
   const float4* __restrict__ plane0 = planes;
   const float4* __restrict__ plane1 = planes + n;
   const float4* __restrict__ plane2 = planes + 2 * size_t(n);
@@ -388,60 +390,60 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
             wind, c.neg_drag, c.neg_lift, s_qa + qi(quad_r, quad_c), s_qb + qi(quad_r, quad_c),
             s_qw + qi(quad_r, quad_c));
   __syncthreads();
-  if (!vertex) return;
+  if (vertex) {
+    // ---- gather in the reference's summation order (grid_order.h)
+    auto take = [&](int kind, int rr, int ccl, int role) {
+      const int i = kind * NO + o(rr, ccl);
+      add_compact(F, s_su[i], s_s2[i], role);
+    };
+    if (INTERIOR) {
+      take(KS, lr - 1, lc, 1);   // SH_UP
+      take(KV, lr - 1, lc, 1);   // VT_UP
+      take(KS, lr, lc - 1, 0);   // SH_LEFT
+      take(KH, lr, lc - 1, 1);   // HZ_LEFT
+      take(KV, lr, lc, 0);       // VT_DOWN
+      take(KH, lr, lc, 0);       // HZ_RIGHT
+      take(KBV, lr - 2, lc, 1);  // BV_UP
+      take(KBH, lr, lc - 2, 1);  // BH_LEFT
+      take(KBH, lr, lc, 0);      // BH_RIGHT
+      take(KBV, lr, lc, 0);      // BV_DOWN
+    } else {
+      for (int j = 0; j < N_SLOTS; ++j) {
+        const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
+        if (owned_exists(d.kind, r + d.dr, cc + d.dc, R, C)) take(d.kind, lr + d.dr, lc + d.dc, d.role);
+      }
+    }
+    for (int sl = 0; sl < N_FACE_SLOTS; ++sl) {
+      const FaceDesc fd = face_desc(sl);
+      if (!INTERIOR && !quad_exists(r + fd.dr, cc + fd.dc, R, C)) continue;
+      const int q = qi(lr + fd.dr, lc + fd.dc);
+      const float4 D = fd.is_b ? s_qb[q] : s_qa[q];
+      float w;
+      if (fd.corner == 0) w = D.w;
+      else if (fd.corner == 1) w = fd.is_b ? s_qw[q].z : s_qw[q].x;
+      else w = fd.is_b ? s_qw[q].w : s_qw[q].y;
+      F = F + w * V3<float>{D.x, D.y, D.z};
+    }
 
-  // ---- gather in the reference's summation order (grid_order.h)
-  auto take = [&](int kind, int rr, int ccl, int role) {
-    const int i = kind * NO + o(rr, ccl);
-    add_compact(F, s_su[i], s_s2[i], role);
-  };
-  if (INTERIOR) {
-    take(KS, lr - 1, lc, 1);   // SH_UP
-    take(KV, lr - 1, lc, 1);   // VT_UP
-    take(KS, lr, lc - 1, 0);   // SH_LEFT
-    take(KH, lr, lc - 1, 1);   // HZ_LEFT
-    take(KV, lr, lc, 0);       // VT_DOWN
-    take(KH, lr, lc, 0);       // HZ_RIGHT
-    take(KBV, lr - 2, lc, 1);  // BV_UP
-    take(KBH, lr, lc - 2, 1);  // BH_LEFT
-    take(KBH, lr, lc, 0);      // BH_RIGHT
-    take(KBV, lr, lc, 0);      // BV_DOWN
-  } else {
-    for (int j = 0; j < N_SLOTS; ++j) {
-      const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
-      if (owned_exists(d.kind, r + d.dr, cc + d.dc, R, C)) take(d.kind, lr + d.dr, lc + d.dc, d.role);
+    // ---- integrate, collide, write
+    const int v = r * C + cc;
+    const float4 P4 = s_pos[e(lr, lc)];
+    const float4 V4 = s_vel[e(lr, lc)];
+    if (V4.w != 0.0f) {  // pinned: update_points restores the old point
+      pos_out[v] = P4;
+      vel_out[v] = V4;
+    } else {
+      const V3<float> P = xyz<float>(P4), V = xyz<float>(V4);
+      const float m = P4.w;
+      V3<float> np, nv, nF;
+      integrate_point<float>(c.integration, c.dt, P, V, F, m, np, nv, nF);
+      collide_point<float>(static_cast<const ObsFace*>(c.obstacle_faces), c.n_obstacle_faces, P, V, F, m, np, nv, c);
+      pos_out[v] = make4<float>(np, m);
+      vel_out[v] = make4<float>(nv, V4.w);
+      const bool bad = !(finite3(np) && finite3(nv));
+      if (__any_sync(__activemask(), bad) && bad && flags) atomicOr(flags, 1u);
     }
   }
-  for (int sl = 0; sl < N_FACE_SLOTS; ++sl) {
-    const FaceDesc fd = face_desc(sl);
-    if (!INTERIOR && !quad_exists(r + fd.dr, cc + fd.dc, R, C)) continue;
-    const int q = qi(lr + fd.dr, lc + fd.dc);
-    const float4 D = fd.is_b ? s_qb[q] : s_qa[q];
-    float w;
-    if (fd.corner == 0) w = D.w;
-    else if (fd.corner == 1) w = fd.is_b ? s_qw[q].z : s_qw[q].x;
-    else w = fd.is_b ? s_qw[q].w : s_qw[q].y;
-    F = F + w * V3<float>{D.x, D.y, D.z};
-  }
-
-  // ---- integrate, collide, write
-  const int v = r * C + cc;
-  const float4 P4 = s_pos[e(lr, lc)];
-  const float4 V4 = s_vel[e(lr, lc)];
-  if (V4.w != 0.0f) {  // pinned: update_points restores the old point
-    pos_out[v] = P4;
-    vel_out[v] = V4;
-    return;
-  }
-  const V3<float> P = xyz<float>(P4), V = xyz<float>(V4);
-  const float m = P4.w;
-  V3<float> np, nv, nF;
-  integrate_point<float>(c.integration, c.dt, P, V, F, m, np, nv, nF);
-  collide_point<float>(static_cast<const ObsFace*>(c.obstacle_faces), c.n_obstacle_faces, P, V, F, m, np, nv, c);
-  pos_out[v] = make4<float>(np, m);
-  vel_out[v] = make4<float>(nv, V4.w);
-  const bool bad = !(finite3(np) && finite3(nv));
-  if (__any_sync(__activemask(), bad) && bad && c.flags) atomicOr(c.flags, 1u);
 }
 
 // One launch for all tiles: the boundary ring first (its tiles are slower
@@ -458,11 +460,44 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
   if (b < n_ring) {
     int bx, by;
     ring_tile(split, b, bx, by);
-    tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c);
+    tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
+                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags);
   } else {
     const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
     tile_step<TW, TH, HALO, true>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel, force_in,
-                                  pos_out, vel_out, c);
+                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags);
+  }
+}
+
+// Many cloths in one launch.  Work items {cloth, tile x, tile y, interior}
+// come from a list packed on the host (largest cloths first, each cloth's
+// boundary tiles before its interior ones); in persistent mode every CTA
+// pulls items from a global counter until the list is exhausted.
+template <int TW, int TH, int HALO>
+__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothDesc* __restrict__ cloths,
+                                                                   const int4* __restrict__ work, int n_work,
+                                                                   int* __restrict__ counter, int parity,
+                                                                   int persistent, StepConsts c) {
+  __shared__ int s_item;
+  int item = blockIdx.x;
+  while (true) {
+    if (persistent) {
+      if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+      __syncthreads();  // also: every thread has finished the previous tile
+      item = s_item;
+      __syncthreads();
+    }
+    if (item >= n_work) break;
+    const int4 w = work[item];
+    const ClothDesc& d = cloths[w.x];
+    const V3<float> wind{d.wind[0], d.wind[1], d.wind[2]};
+    if (w.w)
+      tile_step<TW, TH, HALO, true>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
+                                    d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags);
+    else
+      tile_step<TW, TH, HALO, false>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
+                                     d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags);
+    if (!persistent) break;
   }
 }
 
@@ -475,6 +510,62 @@ size_t tiled_smem_bytes() {
 }
 
 }  // namespace
+
+void batch_tiles(int cloth, int rows, int cols, int* out4, int* n_ring, int* n_interior) {
+  TileSplit t;
+  t.tx = (cols + kTileW - 1) / kTileW;
+  t.ty = (rows + kTileH - 1) / kTileH;
+  t.bx0 = 1;
+  t.bx1 = cols >= kTileW + 4 ? (cols - 2 - kTileW) / kTileW : 0;
+  t.by0 = 1;
+  t.by1 = rows >= kTileH + 4 ? (rows - 2 - kTileH) / kTileH : 0;
+  const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
+  const int ni = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
+  const int nr = t.tx * t.ty - ni;
+  *n_ring = nr;
+  *n_interior = ni;
+  if (!out4) return;
+  int k = 0;
+  for (int by = 0; by < t.ty; ++by)  // ring tiles first
+    for (int bx = 0; bx < t.tx; ++bx) {
+      const bool inner = has_interior && bx >= t.bx0 && bx <= t.bx1 && by >= t.by0 && by <= t.by1;
+      if (inner) continue;
+      out4[4 * k] = cloth; out4[4 * k + 1] = bx; out4[4 * k + 2] = by; out4[4 * k + 3] = 0;
+      ++k;
+    }
+  for (int by = t.by0; has_interior && by <= t.by1; ++by)
+    for (int bx = t.bx0; bx <= t.bx1; ++bx) {
+      out4[4 * k] = cloth; out4[4 * k + 1] = bx; out4[4 * k + 2] = by; out4[4 * k + 3] = 1;
+      ++k;
+    }
+}
+
+int batched_ctas_per_sm() {
+  int n = 0;
+  const size_t smem = tiled_smem_bytes();
+  cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_batched<kTileW, kTileH, kHalo>, kTileW * kTileH + kHalo,
+                                                    smem) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
+                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s) {
+  if (n_work <= 0) return cudaSuccess;
+  const size_t smem = tiled_smem_bytes();
+  static bool attr_set = false;
+  if (!attr_set) {
+    const cudaError_t e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int grid = mode == 1 ? (persistent_ctas < n_work ? persistent_ctas : n_work) : n_work;
+  k_step_batched<kTileW, kTileH, kHalo><<<grid, kTileW * kTileH + kHalo, smem, s>>>(cloths, work, n_work, counter,
+                                                                                    parity, mode == 1, c);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4* vel, const float4* force_in,
                              float4* pos_out, float4* vel_out, const StepConsts& c, cudaStream_t s) {

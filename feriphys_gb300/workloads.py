@@ -163,6 +163,61 @@ def c1(n=1024, side=1.0, dt=1.0 / 600.0, seed=0, noise=1e-3, sphere=(32, 16), in
                  obstacles=obs, rows=n, cols=n)
 
 
+@dataclasses.dataclass
+class Batch:
+    """Many independent cloths (one Simulation, per-cloth wind)."""
+    name: str
+    config: dict
+    cloths: list  # [(cloth_args, pins, wind)]
+    obstacles: list
+
+    @property
+    def n_vertices(self) -> int:
+        return sum(a[0] * a[1] for a, _, _ in self.cloths)
+
+
+def c2(n_cloths=4096, lo=16, hi=128, seed=0, dt=1.0 / 600.0, integration=0) -> Batch:
+    """Batched plain: n_cloths cloths of side U{lo..hi} vertices (1 m side),
+    the small config's strut constants scaled per cloth by U(0.5, 2), pins =
+    one or two random corners or the top row, wind direction uniform on the
+    sphere with speed U(0, 5) m/s, plane collider."""
+    rng = np.random.default_rng(seed)
+    cloths = []
+    for _ in range(n_cloths):
+        n = int(rng.integers(lo, hi + 1))
+        s = 1.0 / (n - 1)
+        lt, ls, lb = s, s * math.sqrt(2.0), 2.0 * s
+        f = float(rng.uniform(0.5, 2.0))
+        args = (n, n, s, (0.0, 0.0, 0.0), 0.01, f * 500.0 * lt, f * 0.5 * lt, f * 250.0 * ls, f * 0.5 * ls,
+                f * 50.0 * lb, f * 0.5 * lb)
+        corners = [n * n - n, n * n - 1, 0, n - 1]
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            pins = [corners[int(rng.integers(0, 4))]]
+        elif kind == 1:
+            pins = [int(x) for x in rng.choice(corners, 2, replace=False)]
+        else:
+            pins = list(range(n * n - n, n * n))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        wind = tuple(float(v) for v in d * rng.uniform(0.0, 5.0))
+        cloths.append((args, np.array(pins, np.uint32), wind))
+    return Batch("c2-%d-cloths" % n_cloths, cloth_config(dt, integration), cloths, [plane(-1.5)])
+
+
+def build_batch(batch: Batch, api):
+    """One Simulation over all cloths of the batch (per-mesh wind)."""
+    meshes = []
+    for args, pins, wind in batch.cloths:
+        m = api.Cloth.new(*args, pins).mesh
+        m.set_wind(wind)
+        meshes.append(m)
+    obstacles = [api.CollidableMesh.new(p, i) for p, i in batch.obstacles]
+    sim = api.Simulation.new(meshes, obstacles)
+    sim.set_config(api.Config.make(**batch.config))
+    return sim, meshes, obstacles
+
+
 def build(scene: Scene, api):
     """Build the scene through a springy API (this package, or the oracle's
     mirror); returns (simulation, mesh, obstacles)."""

@@ -191,6 +191,31 @@ int fgb_sim_get_config(const fgb_sim* s, fgb_config* out);
  * Asynchronous: returns once the launches are queued. */
 int fgb_sim_step(fgb_sim* s, uint64_t n_steps);
 
+/* Per-mesh wind (3 floats), or NULL to use the simulation's Config.wind.
+ * Extension with no reference counterpart: the reference's wind is global
+ * per Simulation (springy/config.rs:13); equivalent to one Simulation per
+ * mesh. */
+int fgb_mesh_set_wind(fgb_mesh* m, const float* wind);
+
+/* Batched stepping: a simulation with two or more Cloth::new grid meshes
+ * advances all of them with one kernel launch per step (largest cloths
+ * first, tiles pulled from a shared work list); a call with n_steps >= 2 is
+ * captured once as a CUDA graph and replayed (1 = default; 0 = plain
+ * launches).  Extension with no reference counterpart (the reference steps
+ * meshes one after another, springy/simulation.rs:28); results are
+ * identical to stepping each mesh alone. */
+int fgb_sim_set_graphs(fgb_sim* s, int enabled);
+
+/* Launch form of the batched step: -1 (default) lets the autotuner choose,
+ * 0 one CTA per tile, 1 persistent CTAs pulling tiles from a work counter. */
+int fgb_sim_set_batch_mode(fgb_sim* s, int mode);
+
+/* out[0] meshes in the batch, out[1] work items (tiles), out[2] launch form
+ * chosen by the autotuner (0 one CTA per tile, 1 persistent; -1 not yet
+ * tuned), out[3] persistent CTAs.  The choice is cached per GPU in
+ * $FGB_AUTOTUNE_CACHE (default ~/.cache/feriphys_gb300/autotune.txt). */
+int fgb_sim_batch_info(const fgb_sim* s, int64_t out[4]);
+
 /* Collision search: 1 (default) uses an exact broad phase over the obstacle
  * faces (candidates visited in face order, so the first hit is unchanged);
  * 0 tests every face for every point like collidable_mesh.rs:107-169.
