@@ -128,6 +128,7 @@ def _declare(l):
         "fgb_sim_set_config": (I, [P, cfg]),
         "fgb_sim_get_config": (I, [P, cfg]),
         "fgb_sim_step": (I, [P, U64]),
+        "fgb_sim_step_static": (I, [P, U64, P]),
         "fgb_sim_set_stream": (I, [P, P]),
         "fgb_sim_set_collision_broadphase": (I, [P, I]),
         "fgb_mesh_set_wind": (I, [P, P]),
@@ -445,6 +446,13 @@ class Simulation:
         """Issue every mesh's work on an external cudaStream_t (an integer
         handle, e.g. torch.cuda.current_stream().cuda_stream); None resets."""
         _check(_lib().fgb_sim_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def step_static(self, n_steps: int = 1, stream_handle=None):
+        """fgb_sim_step_static: the batched step with its scratch in a fixed
+        array, for hosts that cannot allow device allocations after set-up
+        (call ``step(0)`` once during set-up first)."""
+        _check(_lib().fgb_sim_step_static(self._h, int(n_steps),
+                                          C.c_void_p(stream_handle) if stream_handle else None))
 
     def get_timestep(self) -> float:
         s = C.c_double()

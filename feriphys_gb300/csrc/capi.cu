@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <set>
 #include <string>
@@ -1232,3 +1233,144 @@ int fgb_sim_destroy(fgb_sim* s) {
 }
 
 }  // extern "C"
+
+// ===================================================== allocation-free step ===
+//
+// Some hosts cannot let a library allocate device memory once they are
+// running: game engines and renderers that hand out all GPU memory through
+// their own allocators and forbid plugin allocations inside the frame loop,
+// and real-time loops that cannot afford cudaMalloc/cudaFree (both can
+// synchronise the whole device).  fgb_sim_step_static advances a prepared
+// simulation with the batched persistent kernel while keeping that kernel's
+// scratch -- its work counter, the cloth descriptor table and the tile list --
+// in the fixed array below instead of memory allocated for the simulation.
+
+namespace {
+
+// Stated maximum: 4 MiB per GPU, held by every GPU that loads the library.
+constexpr size_t kStaticScratchBytes = size_t(4) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+unsigned char* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device (looked up once
+// per device, with that device current).
+int static_scratch(unsigned char** out) {
+  int dev = 0;
+  FGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(FGB_EINVAL, "device index beyond the supported range");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    FGB_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+    g_static_ptr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_static_ptr[dev];
+  return FGB_OK;
+}
+
+}  // namespace
+
+extern "C" int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream) {
+  if (!s) return fail(FGB_EINVAL, "null sim");
+  if (s->meshes.empty()) return FGB_OK;
+  for (fgb_mesh* m : s->meshes)
+    if (m->topo.rows == 0 || m->path_req == 1 || m->grid_variant != 0 || m->precision != 32)
+      return fail(FGB_EINVAL, "the allocation-free step handles Cloth::new grid meshes on the f32 grid path only");
+  // descriptor table and tile list, largest cloths first (as the batched step)
+  std::vector<fgb_mesh*> order(s->meshes.begin(), s->meshes.end());
+  std::stable_sort(order.begin(), order.end(), [](const fgb_mesh* a, const fgb_mesh* b) { return a->topo.n > b->topo.n; });
+  size_t n_work = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    int nr, ni;
+    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), nullptr, &nr, &ni);
+    n_work += size_t(nr + ni);
+  }
+  const size_t desc_off = 256;
+  const size_t work_off = (desc_off + order.size() * sizeof(fgb::ClothDesc) + 255) & ~size_t(255);
+  const size_t need = work_off + n_work * sizeof(int4);
+  if (need > kStaticScratchBytes)
+    return fail(FGB_EINVAL, "this batch needs " + std::to_string(need) + " bytes of scratch; the allocation-free step "
+                            "holds at most " + std::to_string(kStaticScratchBytes) +
+                            " (" + std::to_string(sizeof(fgb::ClothDesc)) + " bytes per cloth plus 16 bytes per 32x8 tile)");
+  // Everything the step reads must already be on the device: this call
+  // uploads no topology, state or obstacles (that would allocate).
+  if (!s->faces_uploaded)
+    return fail(FGB_ESTATE, "simulation not prepared: call fgb_sim_step(sim, 0) once during set-up");
+  for (fgb_mesh* m : s->meshes) {
+    if (!m->state_on_device || m->topo_dirty || m->pins_dirty || m->staged || m->active_path != 2)
+      return fail(FGB_ESTATE, "mesh not prepared: call fgb_sim_step(sim, 0) once during set-up (and after any "
+                              "topology, pin or precision change)");
+  }
+  FGB_CUDA(cudaSetDevice(s->meshes[0]->device));
+  unsigned char* scratch = nullptr;
+  FGB_CHECK_RC(static_scratch(&scratch));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->meshes[0]->stream;
+
+  std::vector<int> work(4 * n_work);
+  for (size_t i = 0, at = 0; i < order.size(); ++i) {
+    int nr, ni;
+    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), work.data() + 4 * at, &nr, &ni);
+    at += size_t(nr + ni);
+  }
+  for (fgb_mesh* m : order) {  // all cloths read buffer [0] at the first step
+    if (m->stream != st) FGB_CUDA(cudaStreamSynchronize(m->stream));
+    if (m->cur != 0) {
+      std::swap(m->pos[0], m->pos[1]);
+      std::swap(m->vel[0], m->vel[1]);
+      m->cur = 0;
+    }
+  }
+  std::vector<fgb::ClothDesc> desc(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    fgb_mesh* m = order[i];
+    fgb::ClothDesc& d = desc[i];
+    std::memset(&d, 0, sizeof(d));
+    d.planes = m->d_grid;
+    for (int k = 0; k < 2; ++k) {
+      d.pos[k] = static_cast<float4*>(m->pos[k]);
+      d.vel[k] = static_cast<float4*>(m->vel[k]);
+    }
+    d.force_in = m->has_force ? static_cast<const float4*>(m->force) : nullptr;
+    d.flags = m->d_flags;
+    d.rows = int(m->topo.rows);
+    d.cols = int(m->topo.cols);
+    for (int k = 0; k < 3; ++k) d.wind[k] = m->has_wind ? m->wind[k] : s->cfg.wind[k];
+  }
+  fgb::ClothDesc* d_desc = reinterpret_cast<fgb::ClothDesc*>(scratch + desc_off);
+  int4* d_work = reinterpret_cast<int4*>(scratch + work_off);
+  int* d_counter = reinterpret_cast<int*>(scratch);
+  FGB_CUDA(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  int dev = 0, sms = 0;
+  FGB_CUDA(cudaGetDevice(&dev));
+  FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int ctas = fgb::batched_ctas_per_sm() * sms;
+  s->accel.enabled = (s->broadphase && s->d_accel) ? 1 : 0;
+  for (uint64_t k = 0; k < n_steps; ++k) {
+    // the counter keeps the previous call's value: clear it before every launch
+    FGB_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int), st));
+    FGB_CUDA(fgb::launch_step_batched(d_desc, d_work, int(n_work), d_counter, int(k & 1), 1, ctas,
+                                      make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st));
+    if (k == 0 && n_steps > 1) {  // carried forces apply to the first step only
+      bool forces = false;
+      for (const fgb::ClothDesc& d : desc) forces = forces || d.force_in;
+      if (forces) {
+        for (fgb::ClothDesc& d : desc) d.force_in = nullptr;
+        FGB_CUDA(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice,
+                                 st));
+      }
+    }
+  }
+  FGB_CUDA(cudaStreamSynchronize(st));  // the host tables above are released on return
+  for (fgb_mesh* m : order) {
+    m->cur = int(n_steps & 1);
+    m->has_force = m->has_force && n_steps == 0;
+    m->staged = false;
+  }
+  // the batched path's own parity no longer matches these meshes
+  s->batch.clear();
+  return FGB_OK;
+}

@@ -228,6 +228,26 @@ int fgb_sim_set_collision_broadphase(fgb_sim* s, int enabled);
  * step with its own GPU work and time it with its own events. */
 int fgb_sim_set_stream(fgb_sim* s, void* stream);
 
+/* Allocation-free step (no counterpart in the reference).  For hosts that
+ * cannot let a library allocate device memory once they are running -- game
+ * engines and renderers that own all GPU memory through their own
+ * allocators, and real-time loops that cannot afford cudaMalloc/cudaFree,
+ * which may synchronise the whole device.  Advances every mesh of a
+ * simulation n_steps times with the batched persistent kernel, keeping its
+ * scratch (work counter, cloth table, tile list) in a fixed 4 MiB array that
+ * every GPU loading this library holds until exit: it fits 80 bytes per cloth
+ * plus 16 bytes per 32x8 tile (e.g. 4096 cloths of 16..128 vertices a side
+ * need 2.3 MB); larger batches fail with FGB_EINVAL.  Inputs
+ * and outputs are the meshes' device state, as for fgb_sim_step.  All meshes
+ * must be Cloth::new grids on the f32 grid path, already prepared by one
+ * fgb_sim_step(sim, 0) during set-up (else FGB_ESTATE); this call uploads
+ * nothing and allocates nothing.  Its first call on a device looks up the
+ * array's device address, so make that first call before any stream capture.
+ * Every call reuses the same array: calls that overlap on the GPU (other
+ * streams or threads) race.  stream: a cudaStream_t, or NULL for the
+ * simulation's own stream; the call returns when the steps have finished. */
+int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream);
+
 /* Simulation::get_timestep -- springy/simulation.rs:47-49, as
  * Duration::from_secs_f32(dt).as_secs_f64(). */
 int fgb_sim_get_timestep(const fgb_sim* s, double* seconds);
