@@ -261,6 +261,181 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
         dist.destroy_process_group()
 
 
+def rollout_error(p, f):
+    """RMS position difference over the RMS spread of the reference positions."""
+    p, f = p[:, 1:4].astype(np.float64), f[:, 1:4].astype(np.float64)
+    return float(np.sqrt(((p - f) ** 2).sum(1).mean()) / np.sqrt(((f - f.mean(0)) ** 2).sum(1).mean()))
+
+
+SURROGATE_FLOPS_PER_VERTEX = 2 * (54 * 128 + 128 * 128 + 128 * 3)  # 47,360 algorithmic
+SURROGATE_MMA_FLOPS_PER_VERTEX = 2 * (64 * 128 + 128 * 128 + 128 * 16)  # as issued (padded K and N)
+
+
+def run_surrogate(args, rank, world, dist, torch, fgb, W):
+    """c3: the learned surrogate on the 1024^2 cloth; c4: on 4096 uneven cloths.
+
+    The reference's explicit Euler is unstable at dt = 1/600 s on these cloths
+    (the 1024^2 cloth goes non-finite at step 62; at 1/6000 s after ~3,600
+    steps, at any position noise), so the fine solver that generates the
+    training data and judges the surrogate runs at --fine-dt (c3: 1/30000 s,
+    finite through the whole evaluation; c4: 1/6000 s), and one coarse step
+    is `ratio` (10) fine steps.
+    Training data: seeded cloths of the evaluated kind (c3: 256^2 cloths with
+    the large cloth's spacing, stiffness jitter and noise; c4: a 256-cloth
+    batch of the uneven kind), one snapshot every --collect-skip coarse
+    steps, into the device ring.  Then Adam on batches of 65,536 rows.  The
+    evaluation rolls the surrogate out for --coarse-steps coarse steps (with
+    the energy/strain checks and per-cloth fine-step fallback) next to the
+    fine solver over the same simulated time, from the same initial state."""
+    ratio = args.ratio
+    dt_f = args.fine_dt if args.fine_dt > 0 else (1.0 / 30000.0 if args.workload == "c3" else 1.0 / 6000.0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    t_setup = time.perf_counter()
+    sur = fgb.Surrogate.new(1234 + rank)
+    if args.workload == "c3":
+        n = args.n
+        train_side = min(256, n)
+        ring = args.ring
+        sur.reserve(ring)
+        per_cloth = max(1, ring // (args.train_cloths * train_side * train_side))
+        for k in range(args.train_cloths):
+            sc = W.c1(n=train_side, side=(train_side - 1) / (n - 1), dt=dt_f, seed=1000 + k)
+            tsim, _, _ = W.build(sc, fgb)
+            for _ in range(per_cloth):
+                sur.collect(tsim, ratio, 1)
+                tsim.step(ratio * args.collect_skip)
+            del tsim
+        eval_scene = W.c1(n=n, dt=dt_f, seed=rank)
+
+        def build_eval():
+            sim, mesh, _ = W.build(eval_scene, fgb)
+            return sim, [mesh]
+
+        workload = ("c3 surrogate: %dx%d cloth (the plain large config), fine dt=%.3g s Euler, coarse step = %d fine "
+                    "steps; trained on %d seeded %dx%d cloths of the same spacing" % (n, n, dt_f, ratio,
+                                                                                    args.train_cloths, train_side,
+                                                                                    train_side))
+    else:
+        tb = W.c2(n_cloths=args.train_cloths * 64, seed=1000, dt=dt_f)
+        tsim, _, _ = W.build_batch(tb, fgb)
+        ring = args.ring
+        sur.reserve(ring)
+        per = max(1, ring // tb.n_vertices)
+        for _ in range(per):
+            sur.collect(tsim, ratio, 1)
+            tsim.step(ratio * args.collect_skip)
+        del tsim
+        eb = W.c2(n_cloths=args.cloths, seed=rank, dt=dt_f)
+
+        def build_eval():
+            sim, meshes, _ = W.build_batch(eb, fgb)
+            return sim, meshes
+
+        workload = ("c4 batched surrogate: %d uneven cloths (side U{16..128}), fine dt=%.3g s Euler, coarse step = "
+                    "%d fine steps; trained on a %d-cloth batch of the same kind" % (args.cloths, dt_f, ratio,
+                                                                                    args.train_cloths * 64))
+    rows, _ = sur.dataset_info()
+    sur.fit_normalization()
+    collect_s = time.perf_counter() - t_setup
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    a = int(args.train_steps * 2 // 3)
+    losses = np.concatenate([sur.train(a, 65536, 3e-3, seed=1), sur.train(args.train_steps - a, 65536, 1e-3, seed=2)])
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+
+    # fine reference over the same simulated time (timed: one event pair around each coarse interval)
+    psim, pmeshes = build_eval()
+    psim.set_stream(stream.cuda_stream)
+    psim.step(0)
+    n_vert = sum(m.n_points for m in pmeshes)
+    checkpoints = sorted({c for c in (1, 10, 100, args.coarse_steps) if c <= args.coarse_steps})
+    refs = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    done = 0
+    plain_ms = 0.0
+    for c in checkpoints:
+        e0.record(stream)
+        psim.step(ratio * (c - done))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        done = c
+        refs[c] = [m.get_points() for m in pmeshes]
+    plain_fine_ms = plain_ms / (ratio * args.coarse_steps)
+
+    # surrogate: kernel-only timing (no checks), then the checked rollout
+    ssim, smeshes = build_eval()
+    ssim.set_stream(stream.cuda_stream)
+    ssim.step(0)
+    init = [m.get_points() for m in smeshes]
+
+    def reset():
+        for m, p in zip(smeshes, init):
+            m.set_points(p)
+
+    k_kernel = 50
+    ssim.step_surrogate(sur, ratio, 5)
+    reset()
+    e0.record(stream)
+    ssim.step_surrogate(sur, ratio, k_kernel)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kernel_ms = e0.elapsed_time(e1) / k_kernel
+    reset()
+    chk = fgb.SurrogateCheck.make(energy_growth=args.energy_growth, energy_abs=1e-3, max_strain=args.max_strain)
+    errors, fallbacks, done, sur_ms = {}, 0, 0, 0.0
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for c in checkpoints:
+            e0.record(stream)
+            fallbacks += ssim.step_surrogate(sur, ratio, c - done, chk)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sur_ms += e0.elapsed_time(e1)
+            done = c
+            pts = [m.get_points() for m in smeshes]
+            per_cloth = [rollout_error(p, f) if np.isfinite(p).all() else float("inf") for p, f in zip(pts, refs[c])]
+            errors[c] = {"mean": float(np.mean(per_cloth)), "max": float(np.max(per_cloth))}
+    coarse_ms = sur_ms / args.coarse_steps
+    T = ratio * np.float32(dt_f)
+    value = world * n_vert * ratio / (coarse_ms * 1e-3)
+    plain_value = world * n_vert / (plain_fine_ms * 1e-3)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
+    peak = peaks["bf16_tflops"] if peaks else 1900.0
+    achieved = SURROGATE_FLOPS_PER_VERTEX * n_vert / (kernel_ms * 1e-3) / 1e12
+    if rank == 0:
+        print(json.dumps({
+            "metric": "cloth vertex-steps/s (fine-step equivalents) with the learned surrogate", "value": value,
+            "unit": UNIT, "n_gpus": world, "steps": args.coarse_steps, "warmup": 5,
+            "ms_per_step": coarse_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 (MLP, f32 accumulate) / f32 (state)", "data": "synthetic (seeded)",
+            "config": {"workload": workload, "vertices": n_vert, "ratio": ratio, "coarse_dt": float(T),
+                       "fine_dt": dt_f, "checks": {"energy_growth": args.energy_growth, "max_strain": args.max_strain},
+                       "l2": "working set larger than L2 (c4) / one cloth of 1M vertices (c3): not flushed"},
+            "error_vs_fine": {str(k): v for k, v in errors.items()},
+            "fallbacks": fallbacks,
+            "simulated_seconds_per_s": {"surrogate": float(T) / (coarse_ms * 1e-3),
+                                        "plain_fine": dt_f / (plain_fine_ms * 1e-3),
+                                        "ratio": (float(T) / coarse_ms) / (dt_f / plain_fine_ms)},
+            "plain_fine_vertex_steps_per_s": plain_value,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "algorithmic_flops_per_launch": SURROGATE_FLOPS_PER_VERTEX * n_vert,
+                         "kernel_ms": kernel_ms,
+                         "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch"},
+            "training": {"rows": rows, "collect_and_setup_s": collect_s, "steps": int(args.train_steps),
+                         "batch": 65536, "seconds": train_s, "samples_per_s": args.train_steps * 65536 / train_s,
+                         "loss_first": float(losses[0]), "loss_last": float(losses[-1])},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": None,
+            "clocks": clk.summary(), "device": torch.cuda.get_device_name()}), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,9 +449,19 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general gather, 2 tiled grid, 3 untiled grid")
     ap.add_argument("--probe", action="store_true", help="report the first step whose state is non-finite")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2"],
-                    help="c1: one 1024x1024 cloth (default); c2: 4096 uneven cloths, one launch per step")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
+                    help="c1: one 1024x1024 cloth (default); c2: 4096 uneven cloths, one launch per step; "
+                         "c3/c4: the learned surrogate on c1/c2")
     ap.add_argument("--cloths", type=int, default=4096)
+    ap.add_argument("--ratio", type=int, default=10, help="fine steps per surrogate coarse step")
+    ap.add_argument("--coarse-steps", type=int, default=1000)
+    ap.add_argument("--fine-dt", type=float, default=0.0, help="fine step of the surrogate workloads (0: default)")
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-cloths", type=int, default=4)
+    ap.add_argument("--ring", type=int, default=4 * 1024 * 1024, help="dataset ring rows")
+    ap.add_argument("--collect-skip", type=int, default=60, help="coarse steps between collected snapshots")
+    ap.add_argument("--energy-growth", type=float, default=0.05)
+    ap.add_argument("--max-strain", type=float, default=100.0)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -308,6 +493,8 @@ def main():
 
     if args.workload == "c2":
         return run_batched(args, rank, world, dist, torch, fgb, W)
+    if args.workload in ("c3", "c4"):
+        return run_surrogate(args, rank, world, dist, torch, fgb, W)
 
     scene = W.c1(n=args.n, seed=rank)
     sim, mesh, _ = W.build(scene, fgb)

@@ -28,7 +28,10 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Integration", "Config", "SpringyMesh", "Cloth", "CollidableMesh", "Simulation", "FgbError",
-           "library_path", "POINT_FIELDS"]
+           "Surrogate", "SurrogateCheck", "library_path", "POINT_FIELDS", "N_FEATURES", "N_PARAMS"]
+
+N_FEATURES = 54
+N_PARAMS = 128 * 54 + 128 + 128 * 128 + 128 + 3 * 128 + 3
 
 POINT_FIELDS = ("mass", "px", "py", "pz", "vx", "vy", "vz", "fx", "fy", "fz")
 
@@ -78,6 +81,21 @@ class Config(C.Structure):
         c.coefficient_of_restitution = float(coefficient_of_restitution)
         c.coefficient_of_friction = float(coefficient_of_friction)
         return c
+
+
+class SurrogateCheck(C.Structure):
+    """fgb_surrogate_check: per-cloth energy and strain limits of a coarse step."""
+
+    _fields_ = [
+        ("enabled", C.c_int32),
+        ("energy_growth", C.c_float),
+        ("energy_abs", C.c_float),
+        ("max_strain", C.c_float),
+    ]
+
+    @classmethod
+    def make(cls, energy_growth=0.05, energy_abs=1e-3, max_strain=0.25, enabled=True) -> "SurrogateCheck":
+        return cls(1 if enabled else 0, energy_growth, energy_abs, max_strain)
 
 
 class _Override(C.Structure):
@@ -138,6 +156,24 @@ def _declare(l):
         "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
         "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
         "fgb_sim_destroy": (I, [P]),
+        "fgb_surrogate_new": (I, [U64, pp]),
+        "fgb_surrogate_destroy": (I, [P]),
+        "fgb_surrogate_get_params": (I, [P, P]),
+        "fgb_surrogate_set_params": (I, [P, P]),
+        "fgb_surrogate_set_normalization": (I, [P, P, P, P, P]),
+        "fgb_surrogate_get_normalization": (I, [P, P, P, P, P]),
+        "fgb_surrogate_features": (I, [P, P, F, P, P]),
+        "fgb_surrogate_forward": (I, [P, P, U64, P]),
+        "fgb_surrogate_gradients": (I, [P, P, P, U64, P, P]),
+        "fgb_surrogate_train_batch": (I, [P, P, P, U64, F, P]),
+        "fgb_surrogate_dataset_reserve": (I, [P, U64]),
+        "fgb_surrogate_collect": (I, [P, P, U32, U64]),
+        "fgb_surrogate_dataset_info": (I, [P, P]),
+        "fgb_surrogate_dataset_get": (I, [P, U64, U64, P, P]),
+        "fgb_surrogate_fit_normalization": (I, [P]),
+        "fgb_surrogate_train": (I, [P, U64, U64, F, U64, P]),
+        "fgb_sim_step_surrogate": (I, [P, P, U32, U64, C.POINTER(SurrogateCheck), C.POINTER(C.c_uint64)]),
+        "fgb_sim_energy": (I, [P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(l, name)
@@ -470,3 +506,115 @@ class Simulation:
         bad = C.c_int()
         _check(_lib().fgb_sim_synchronize(self._h, C.byref(bad)))
         return bool(bad.value)
+
+    def step_surrogate(self, surrogate: "Surrogate", ratio: int, n_coarse: int = 1, check=None) -> int:
+        """n_coarse coarse steps of ratio fine steps each with the learned
+        surrogate; with a SurrogateCheck, failing cloths fall back to the fine
+        step.  Returns the number of fallbacks."""
+        n = C.c_uint64()
+        _check(_lib().fgb_sim_step_surrogate(self._h, surrogate._h, int(ratio), int(n_coarse),
+                                             C.byref(check) if check is not None else None, C.byref(n)))
+        return int(n.value)
+
+    def energy(self) -> np.ndarray:
+        """[n_meshes, 2]: energy and maximum strain of each mesh's state."""
+        out = np.zeros((len(self._meshes), 2), np.float32)
+        _check(_lib().fgb_sim_energy(self._h, _ptr(out)))
+        return out
+
+
+class Surrogate:
+    """Learned per-vertex surrogate of the cloth step (no reference
+    counterpart): MLP 54 -> 128 -> 128 -> 3 trained and run by CUDA kernels
+    (tcgen05 tensor cores, bf16 weights, f32 accumulation)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def new(cls, seed: int = 0) -> "Surrogate":
+        h = C.c_void_p()
+        _check(_lib().fgb_surrogate_new(int(seed), C.byref(h)))
+        return cls(h.value)
+
+    def __del__(self):
+        try:
+            if self._h and _LIB is not None:
+                _LIB.fgb_surrogate_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(N_PARAMS, np.float32)
+        _check(_lib().fgb_surrogate_get_params(self._h, _ptr(out)))
+        return out
+
+    def set_params(self, params):
+        p = _f32(params)
+        if p.size != N_PARAMS:
+            raise ValueError("expected %d parameters" % N_PARAMS)
+        _check(_lib().fgb_surrogate_set_params(self._h, _ptr(p)))
+
+    def set_normalization(self, in_mean, in_std, out_mean, out_std):
+        a, b, c, d = _f32(in_mean), _f32(in_std), _f32(out_mean), _f32(out_std)
+        _check(_lib().fgb_surrogate_set_normalization(self._h, _ptr(a), _ptr(b), _ptr(c), _ptr(d)))
+
+    def get_normalization(self):
+        a, b = np.zeros(N_FEATURES, np.float32), np.zeros(N_FEATURES, np.float32)
+        c, d = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        _check(_lib().fgb_surrogate_get_normalization(self._h, _ptr(a), _ptr(b), _ptr(c), _ptr(d)))
+        return a, b, c, d
+
+    def features(self, mesh: SpringyMesh, coarse_dt: float, wind=None) -> np.ndarray:
+        n = mesh.n_points
+        out = np.zeros((n, N_FEATURES), np.float32)
+        w = None if wind is None else _f32(wind)
+        _check(_lib().fgb_surrogate_features(self._h, mesh._h, float(coarse_dt), _ptr(w), _ptr(out)))
+        return out
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, N_FEATURES))
+        y = np.zeros((x.shape[0], 3), np.float32)
+        _check(_lib().fgb_surrogate_forward(self._h, _ptr(x), x.shape[0], _ptr(y)))
+        return y
+
+    def gradients(self, x, t):
+        x = np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, N_FEATURES))
+        t = np.ascontiguousarray(np.asarray(t, np.float32).reshape(-1, 3))
+        g = np.zeros(N_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(_lib().fgb_surrogate_gradients(self._h, _ptr(x), _ptr(t), x.shape[0], _ptr(g), C.byref(loss)))
+        return g, float(loss.value)
+
+    def train_batch(self, x, t, lr: float) -> float:
+        x = np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, N_FEATURES))
+        t = np.ascontiguousarray(np.asarray(t, np.float32).reshape(-1, 3))
+        loss = C.c_float()
+        _check(_lib().fgb_surrogate_train_batch(self._h, _ptr(x), _ptr(t), x.shape[0], float(lr), C.byref(loss)))
+        return float(loss.value)
+
+    def reserve(self, capacity_rows: int):
+        _check(_lib().fgb_surrogate_dataset_reserve(self._h, int(capacity_rows)))
+
+    def collect(self, sim: Simulation, ratio: int, n_coarse: int):
+        _check(_lib().fgb_surrogate_collect(self._h, sim._h, int(ratio), int(n_coarse)))
+
+    def dataset_info(self):
+        out = np.zeros(2, np.uint64)
+        _check(_lib().fgb_surrogate_dataset_info(self._h, _ptr(out)))
+        return int(out[0]), int(out[1])
+
+    def dataset(self, first: int, n: int):
+        f = np.zeros((n, N_FEATURES), np.float32)
+        t = np.zeros((n, 3), np.float32)
+        _check(_lib().fgb_surrogate_dataset_get(self._h, int(first), int(n), _ptr(f), _ptr(t)))
+        return f, t
+
+    def fit_normalization(self):
+        _check(_lib().fgb_surrogate_fit_normalization(self._h))
+
+    def train(self, n_steps: int, batch: int = 65536, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        losses = np.zeros(max(1, int(n_steps)), np.float32)
+        _check(_lib().fgb_surrogate_train(self._h, int(n_steps), int(batch), float(lr), int(seed), _ptr(losses)))
+        return losses[: int(n_steps)]

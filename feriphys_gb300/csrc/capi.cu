@@ -18,22 +18,25 @@
 #include <sys/stat.h>
 
 #include "feriphys_gb300.h"
+#include "handles.h"
 #include "kernels.h"
 #include "mesh_build.h"
 #include "obstacle_accel.h"
 #include "physics.cuh"
 #include "state_io.h"
 
-using fgb::MeshTopo;
-
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
-int fail(int code, const std::string& msg) {
+int fgb::detail::fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+using fgb::detail::fail;
+
+namespace {
 
 #define FGB_CUDA(call)                                                                              \
   do {                                                                                              \
@@ -66,98 +69,6 @@ cudaError_t dalloc(P*& p, size_t bytes) {
 bool finite_nonneg(float x) { return std::isfinite(x) && x >= 0.0f; }
 
 }  // namespace
-
-// A library-created stream shared by every mesh that issues work on it (all
-// meshes of a batched simulation share one); destroyed with its last user.
-struct StreamOwner {
-  cudaStream_t s = nullptr;
-  ~StreamOwner() {
-    if (s) cudaStreamDestroy(s);
-  }
-};
-
-struct fgb_obstacle {
-  uint64_t n_vertices = 0;
-  uint64_t n_edges = 0;
-  std::vector<fgb::ObsFace> faces;  // device layout, computed on the host
-};
-
-struct fgb_mesh {
-  MeshTopo topo;
-  int device = 0;
-  int path_req = 0;      // 0 auto, 1 general, 2 grid
-  int grid_variant = 0;  // 0 tiled grid kernel, 1 per-vertex grid kernel
-  int precision = 32;    // 32 or 64
-  int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
-  cudaStream_t stream = nullptr;      // the stream all work of this mesh is issued on
-  std::shared_ptr<StreamOwner> own;   // library stream (possibly shared with a batch)
-  bool external_stream = false;
-  float wind[3] = {0, 0, 0};          // per-mesh wind (extension), used when has_wind
-  bool has_wind = false;
-
-  // host copy of the state while the device does not hold it (as_state layout)
-  std::vector<float> host_pts;
-  bool state_on_device = false;
-  bool topo_dirty = true;
-  bool pins_dirty = true;
-  bool csr_ready = false;
-
-  // device state
-  void* pos[2] = {nullptr, nullptr};
-  void* vel[2] = {nullptr, nullptr};
-  int cur = 0;
-  void* force = nullptr;
-  bool has_force = false;  // force buffer holds the points' accumulated force
-  void* spos = nullptr;
-  void* svel = nullptr;
-  void* sforce = nullptr;
-  bool staged = false;
-  float* d_io = nullptr;  // as_state staging (10 floats per point; doubles for f64 readback)
-  size_t d_io_bytes = 0;
-  uint8_t* d_pinned = nullptr;
-  unsigned* d_flags = nullptr;
-
-  // general topology
-  int* d_strut_off = nullptr;
-  int2* d_strut_inc = nullptr;
-  float4* d_strut_kcl = nullptr;
-  int* d_face_off = nullptr;
-  int* d_face_inc = nullptr;
-  int4* d_face_vtx = nullptr;
-  // grid topology
-  float4* d_grid = nullptr;
-
-  size_t elem() const { return precision == 64 ? sizeof(fgb::Dbl4) : sizeof(float4); }
-};
-
-struct fgb_sim {
-  std::vector<fgb_mesh*> meshes;
-  std::vector<fgb_obstacle*> obstacles;
-  fgb_config cfg;
-  std::vector<fgb::ObsFace> faces;  // flattened obstacle faces (uploaded at the first step)
-  fgb::ObsFace* d_faces = nullptr;
-  int n_faces = 0;
-  bool faces_uploaded = false;
-  bool broadphase = true;
-  fgb::ObsAccel accel{};  // device broad phase (pointers into d_accel)
-  int* d_accel = nullptr;
-  // batched stepping of grid meshes (two or more): one kernel per step
-  std::vector<fgb_mesh*> batch;           // grid meshes, largest first
-  std::vector<fgb::ClothDesc> desc;       // host copy of the device table
-  fgb::ClothDesc* d_desc = nullptr;
-  size_t d_desc_cap = 0;
-  int4* d_work = nullptr;
-  int n_work = 0;
-  int* d_counter = nullptr;
-  int parity = 0;
-  int mode = -1, ctas = 0;                // launch form chosen by the tuner
-  int forced_mode = -1;                   // fgb_sim_set_batch_mode (-1: tuner)
-  bool graphs = true;
-  std::map<std::pair<uint64_t, int>, cudaGraphExec_t> graph_cache;
-  fgb_config graph_cfg;
-  std::shared_ptr<StreamOwner> stream;    // shared with the batch's meshes
-  cudaStream_t ext_stream = nullptr;      // caller's stream (fgb_sim_set_stream), if any
-};
 
 namespace {
 
@@ -657,6 +568,48 @@ int make_obstacle_faces(fgb_obstacle* const* obs, uint64_t nobs, std::vector<fgb
 
 }  // namespace
 
+namespace {
+
+// Obstacle faces and their broad phase on the device (once per simulation).
+int upload_faces(fgb_sim* s) {
+  if (!s->faces_uploaded) {
+    if (!s->faces.empty()) {
+      FGB_CUDA(dalloc(s->d_faces, s->faces.size() * sizeof(fgb::ObsFace)));
+      FGB_CUDA(cudaMemcpy(s->d_faces, s->faces.data(), s->faces.size() * sizeof(fgb::ObsFace),
+                          cudaMemcpyHostToDevice));
+      std::vector<int> first, count;
+      int base = 0;
+      for (fgb_obstacle* o : s->obstacles) {
+        first.push_back(base);
+        count.push_back(int(o->faces.size()));
+        base += int(o->faces.size());
+      }
+      fgb::AccelHost a;
+      fgb::build_obstacle_accel(s->faces, first, count, a);
+      const size_t n_off = a.cell_off.size(), n_cf = a.cell_faces.size(), n_al = a.always.size();
+      const size_t n_grid_ints = a.grids.size() * sizeof(fgb::ObsGrid3) / sizeof(int);
+      FGB_CUDA(dalloc(s->d_accel, (n_off + n_cf + n_al + n_grid_ints + 4) * sizeof(int)));
+      FGB_CUDA(cudaMemcpy(s->d_accel, a.cell_off.data(), n_off * sizeof(int), cudaMemcpyHostToDevice));
+      FGB_CUDA(cudaMemcpy(s->d_accel + n_off, a.cell_faces.data(), n_cf * sizeof(int), cudaMemcpyHostToDevice));
+      FGB_CUDA(cudaMemcpy(s->d_accel + n_off + n_cf, a.always.data(), n_al * sizeof(int), cudaMemcpyHostToDevice));
+      // grid descriptors last, 16-byte aligned
+      const size_t gofs = (n_off + n_cf + n_al + 3) & ~size_t(3);
+      FGB_CUDA(cudaMemcpy(s->d_accel + gofs, a.grids.data(), a.grids.size() * sizeof(fgb::ObsGrid3),
+                          cudaMemcpyHostToDevice));
+      s->accel.cell_off = s->d_accel;
+      s->accel.cell_faces = s->d_accel + n_off;
+      s->accel.always = s->d_accel + n_off + n_cf;
+      s->accel.grids = reinterpret_cast<const fgb::ObsGrid3*>(s->d_accel + gofs);
+      s->accel.n_grids = int(a.grids.size());
+    }
+    s->faces_uploaded = true;
+  }
+  s->accel.enabled = (s->broadphase && s->d_accel) ? 1 : 0;
+  return FGB_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* fgb_last_error(void) { return g_err.c_str(); }
@@ -1098,39 +1051,7 @@ int fgb_sim_get_config(const fgb_sim* s, fgb_config* out) {
 
 int fgb_sim_step(fgb_sim* s, uint64_t n_steps) {
   if (!s) return fail(FGB_EINVAL, "null sim");
-  if (!s->faces_uploaded) {
-    if (!s->faces.empty()) {
-      FGB_CUDA(dalloc(s->d_faces, s->faces.size() * sizeof(fgb::ObsFace)));
-      FGB_CUDA(cudaMemcpy(s->d_faces, s->faces.data(), s->faces.size() * sizeof(fgb::ObsFace),
-                          cudaMemcpyHostToDevice));
-      std::vector<int> first, count;
-      int base = 0;
-      for (fgb_obstacle* o : s->obstacles) {
-        first.push_back(base);
-        count.push_back(int(o->faces.size()));
-        base += int(o->faces.size());
-      }
-      fgb::AccelHost a;
-      fgb::build_obstacle_accel(s->faces, first, count, a);
-      const size_t n_off = a.cell_off.size(), n_cf = a.cell_faces.size(), n_al = a.always.size();
-      const size_t n_grid_ints = a.grids.size() * sizeof(fgb::ObsGrid3) / sizeof(int);
-      FGB_CUDA(dalloc(s->d_accel, (n_off + n_cf + n_al + n_grid_ints + 4) * sizeof(int)));
-      FGB_CUDA(cudaMemcpy(s->d_accel, a.cell_off.data(), n_off * sizeof(int), cudaMemcpyHostToDevice));
-      FGB_CUDA(cudaMemcpy(s->d_accel + n_off, a.cell_faces.data(), n_cf * sizeof(int), cudaMemcpyHostToDevice));
-      FGB_CUDA(cudaMemcpy(s->d_accel + n_off + n_cf, a.always.data(), n_al * sizeof(int), cudaMemcpyHostToDevice));
-      // grid descriptors last, 16-byte aligned
-      const size_t gofs = (n_off + n_cf + n_al + 3) & ~size_t(3);
-      FGB_CUDA(cudaMemcpy(s->d_accel + gofs, a.grids.data(), a.grids.size() * sizeof(fgb::ObsGrid3),
-                          cudaMemcpyHostToDevice));
-      s->accel.cell_off = s->d_accel;
-      s->accel.cell_faces = s->d_accel + n_off;
-      s->accel.always = s->d_accel + n_off + n_cf;
-      s->accel.grids = reinterpret_cast<const fgb::ObsGrid3*>(s->d_accel + gofs);
-      s->accel.n_grids = int(a.grids.size());
-    }
-    s->faces_uploaded = true;
-  }
-  s->accel.enabled = (s->broadphase && s->d_accel) ? 1 : 0;
+  FGB_CHECK_RC(upload_faces(s));
   for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_device(m));
   FGB_CHECK_RC(prepare_batch(s));
   if (!s->batch.empty()) FGB_CHECK_RC(batched_steps(s, n_steps));
@@ -1233,6 +1154,24 @@ int fgb_sim_destroy(fgb_sim* s) {
 }
 
 }  // extern "C"
+
+int fgb::detail::ensure_device(fgb_mesh* m) { return ::ensure_device(m); }
+
+fgb::StepConsts fgb::detail::make_consts(const fgb_config& cfg, const fgb::ObsFace* faces, int n_faces,
+                                         unsigned* flags, const fgb::ObsAccel* accel) {
+  return ::make_consts(cfg, faces, n_faces, flags, accel);
+}
+
+int fgb::detail::ensure_sim(fgb_sim* s) {
+  FGB_CHECK_RC(upload_faces(s));
+  for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(::ensure_device(m));
+  return prepare_batch(s);
+}
+
+cudaStream_t fgb::detail::sim_stream(fgb_sim* s) {
+  if (!s->batch.empty()) return batch_stream(s);
+  return s->meshes.empty() ? nullptr : s->meshes[0]->stream;
+}
 
 // ===================================================== allocation-free step ===
 //

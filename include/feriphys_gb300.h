@@ -258,6 +258,85 @@ int fgb_sim_synchronize(fgb_sim* s, int* nonfinite);
 
 int fgb_sim_destroy(fgb_sim* s);
 
+
+/* ---- Learned surrogate (no counterpart in the reference) -----------------
+ * A per-vertex MLP 54 -> 128 -> 128 -> 3 (tanh-form GELU, bf16 weights, f32
+ * accumulation on the tensor cores) that predicts, for a vertex of a
+ * Cloth::new grid, its velocity change over one coarse step of `ratio` fine
+ * steps of the simulation's dt, from its 8-neighbour stencil (relative
+ * positions and velocities), pin flag, relative wind and normal.  Training
+ * data comes from the simulation's own fine steps on the GPU; training
+ * (forward, backward, Adam) and inference are CUDA kernels of this library.
+ * The fine step stays the judge: fgb_sim_step_surrogate checks each cloth's
+ * energy and maximum strain after every coarse step and reverts a failing
+ * cloth to `ratio` fine steps.
+ *
+ * Public parameter layout (f32, row-major, rows = outputs): W1[128][54],
+ * b1[128], W2[128][128], b2[128], W3[3][128], b3[3] (23939 floats).
+ * The network sees standardised inputs (x - in_mean) / in_std and predicts
+ * standardised outputs; y * out_std + out_mean is the velocity change times
+ * T / h (T the coarse step, h the cloth's rest spacing). */
+typedef struct fgb_surrogate fgb_surrogate;
+
+typedef struct fgb_surrogate_check {
+  int32_t enabled;      /* 0: no checks, no fallback                                   */
+  float energy_growth;  /* fail when E_new > E_old + energy_growth * |E_old| + energy_abs */
+  float energy_abs;     /* J                                                             */
+  float max_strain;     /* fail when any strut's |(|d| - L) / L| exceeds this            */
+} fgb_surrogate_check;
+
+/* New network on the current device: Xavier-uniform weights from `seed`,
+ * zero biases, identity normalisation, empty dataset. */
+int fgb_surrogate_new(uint64_t seed, fgb_surrogate** out);
+int fgb_surrogate_destroy(fgb_surrogate* g);
+int fgb_surrogate_get_params(fgb_surrogate* g, float* out /* 23939 */);
+int fgb_surrogate_set_params(fgb_surrogate* g, const float* in /* 23939 */);
+/* in_mean[54], in_std[54], out_mean[3], out_std[3]; any may be NULL on get. */
+int fgb_surrogate_set_normalization(fgb_surrogate* g, const float* in_mean, const float* in_std,
+                                    const float* out_mean, const float* out_std);
+int fgb_surrogate_get_normalization(const fgb_surrogate* g, float* in_mean, float* in_std, float* out_mean,
+                                    float* out_std);
+/* Raw (unstandardised) inputs of every vertex of a grid mesh for coarse step
+ * `coarse_dt` and wind `wind[3]` (NULL: the mesh's wind or zero): out[n][54]. */
+int fgb_surrogate_features(fgb_surrogate* g, fgb_mesh* m, float coarse_dt, const float* wind, float* out);
+/* Network outputs y[n][3] for standardised inputs x[n][54] (host buffers). */
+int fgb_surrogate_forward(fgb_surrogate* g, const float* x, uint64_t n, float* y);
+/* Gradient of the mean squared error mean((y - t)^2) over n rows (n a
+ * multiple of 128) in the public layout; *loss = that mean.  Nothing changes. */
+int fgb_surrogate_gradients(fgb_surrogate* g, const float* x, const float* t, uint64_t n, float* grad, float* loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on host rows; *loss = the
+ * batch's mean squared error before the step. */
+int fgb_surrogate_train_batch(fgb_surrogate* g, const float* x, const float* t, uint64_t n, float lr, float* loss);
+/* Device ring of training transitions (one row per vertex and coarse step). */
+int fgb_surrogate_dataset_reserve(fgb_surrogate* g, uint64_t capacity_rows);
+/* Runs n_coarse x ratio fine steps of the simulation (fgb_sim_step) and
+ * records, before each coarse step, every vertex's inputs and, after it, its
+ * velocity change; the oldest rows are overwritten when the ring is full. */
+int fgb_surrogate_collect(fgb_surrogate* g, fgb_sim* s, uint32_t ratio, uint64_t n_coarse);
+/* out[0] = rows held, out[1] = capacity. */
+int fgb_surrogate_dataset_info(const fgb_surrogate* g, uint64_t out[2]);
+/* Copies rows [first, first + n) of the ring: feat[n][54], tgt[n][3]. */
+int fgb_surrogate_dataset_get(fgb_surrogate* g, uint64_t first, uint64_t n, float* feat, float* tgt);
+/* Sets the normalisation to the dataset's per-feature mean and standard
+ * deviation (a standard deviation below 1e-6 becomes 1). */
+int fgb_surrogate_fit_normalization(fgb_surrogate* g);
+/* n_steps Adam steps on batches of `batch` rows (a multiple of 128) drawn
+ * from the dataset with a seeded hash; losses[n_steps] (may be NULL). */
+int fgb_surrogate_train(fgb_surrogate* g, uint64_t n_steps, uint64_t batch, float lr, uint64_t seed,
+                        float* losses);
+
+/* n_coarse coarse steps of every mesh (all Cloth::new grids on the f32 grid
+ * path) with the surrogate: T = ratio * dt, v' = v + dv, p' = p + (v + v') T / 2,
+ * collision response against the obstacles over T, pinned vertices
+ * unchanged.  With chk->enabled, a cloth whose energy or strain check fails
+ * after a coarse step is reverted and advanced by `ratio` fine steps instead;
+ * *n_fallbacks (may be NULL) receives the number of such reverts. */
+int fgb_sim_step_surrogate(fgb_sim* s, fgb_surrogate* g, uint32_t ratio, uint64_t n_coarse,
+                           const fgb_surrogate_check* chk, uint64_t* n_fallbacks);
+/* Energy and maximum strain of each mesh's current state (out[2 * n_meshes]),
+ * as the checks compute them. */
+int fgb_sim_energy(fgb_sim* s, float* out);
+
 #ifdef __cplusplus
 }
 #endif
