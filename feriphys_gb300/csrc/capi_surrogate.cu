@@ -93,6 +93,8 @@ struct fgb_surrogate {
   size_t cloth_chk_cap = 0;
   float* d_out = nullptr;
   size_t out_cap = 0;
+  fgb::ClothDesc* d_fdesc = nullptr;  // batched fine-step fallback table (batch order, skip flags)
+  size_t fdesc_cap = 0;
   int groups = 4;
 };
 
@@ -324,6 +326,63 @@ int run_check(fgb_surrogate* g, fgb_sim* s, int n_tiles, int parity, std::vector
   return FGB_OK;
 }
 
+// `ratio` fine steps of the meshes in `failing` (indices into s->meshes),
+// starting from buffers [par] and ending in [par ^ 1], the other meshes
+// untouched.  Single meshes step with the grid kernel; a batch with one
+// masked launch of the batched kernel per fine step.
+int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing, int par, uint32_t ratio,
+                  cudaStream_t st) {
+  const fgb::StepConsts fc = fgb::detail::make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel);
+  if (s->batch.empty()) {
+    for (int c : failing) {
+      fgb_mesh* m = s->meshes[c];
+      const fgb::GridTopo gt{int(m->topo.rows), int(m->topo.cols), m->d_grid, 0};
+      fgb::StepConsts mc = fc;
+      mc.flags = m->d_flags;
+      int a = par;
+      for (uint32_t j = 0; j < ratio; ++j, a ^= 1)
+        FGB_CUDA(fgb::launch_step_grid(gt, static_cast<const float4*>(m->pos[a]), static_cast<const float4*>(m->vel[a]),
+                                       nullptr, static_cast<float4*>(m->pos[a ^ 1]), static_cast<float4*>(m->vel[a ^ 1]),
+                                       mc, st));
+      if (a != (par ^ 1)) {
+        const size_t bytes = size_t(m->topo.n) * sizeof(float4);
+        FGB_CUDA(cudaMemcpyAsync(m->pos[par ^ 1], m->pos[a], bytes, cudaMemcpyDeviceToDevice, st));
+        FGB_CUDA(cudaMemcpyAsync(m->vel[par ^ 1], m->vel[a], bytes, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+    return FGB_OK;
+  }
+  std::vector<char> fail_mesh(s->meshes.size(), 0);
+  for (int c : failing) fail_mesh[c] = 1;
+  std::vector<fgb::ClothDesc> d = s->desc;
+  for (size_t b = 0; b < s->batch.size(); ++b) {
+    const size_t mi = size_t(std::find(s->meshes.begin(), s->meshes.end(), s->batch[b]) - s->meshes.begin());
+    d[b].skip = (mi < fail_mesh.size() && fail_mesh[mi]) ? 0 : 1;
+    d[b].force_in = nullptr;
+  }
+  FGB_CUDA(dgrow(g->d_fdesc, g->fdesc_cap, d.size(), sizeof(fgb::ClothDesc)));
+  FGB_CUDA(cudaMemcpyAsync(g->d_fdesc, d.data(), d.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice, st));
+  int from = par;
+  if ((ratio & 1u) == 0) {
+    FGB_CUDA(S::launch_copy_unskipped(g->d_fdesc, int(d.size()), par, st));
+    from = par ^ 1;
+  }
+  int ctas = s->ctas;
+  if (s->mode != 1 || ctas <= 0) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ctas = fgb::batched_ctas_per_sm() * sms;
+  }
+  for (uint32_t j = 0; j < ratio; ++j) {
+    FGB_CUDA(cudaMemsetAsync(s->d_counter, 0, sizeof(int), st));
+    FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, s->d_work, s->n_work, s->d_counter, from ^ int(j & 1u), 1, ctas, fc,
+                                      st));
+  }
+  FGB_CUDA(cudaStreamSynchronize(st));  // the host table must outlive its upload
+  return FGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -401,6 +460,7 @@ int fgb_surrogate_destroy(fgb_surrogate* g) {
   dfree(g->d_tile_chk);
   dfree(g->d_cloth_chk);
   dfree(g->d_out);
+  dfree(g->d_fdesc);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
   return FGB_OK;
@@ -656,36 +716,35 @@ int fgb_sim_step_surrogate(fgb_sim* s, fgb_surrogate* g, uint32_t ratio, uint64_
   const fgb::StepConsts cst = fgb::detail::make_consts(cc, s->d_faces, s->n_faces, nullptr, &s->accel);
   const bool checks = chk && chk->enabled;
   std::vector<float2> e_old, e_new;
+  std::vector<double> e_ref(s->meshes.size());
+  {
+    const double gmag = std::sqrt(double(s->cfg.gravity[0]) * s->cfg.gravity[0] +
+                                  double(s->cfg.gravity[1]) * s->cfg.gravity[1] +
+                                  double(s->cfg.gravity[2]) * s->cfg.gravity[2]);
+    for (size_t c = 0; c < s->meshes.size(); ++c)
+      e_ref[c] = double(s->meshes[c]->topo.n) * gmag * double(mesh_spacing(s->meshes[c]));
+  }
   if (checks) FGB_CHECK_RC(run_check(g, s, n_tiles, s->parity, e_old, st));
   uint64_t fallbacks = 0;
+  std::vector<int> failing;
   for (uint64_t k = 0; k < n_coarse; ++k) {
     const int par = s->parity;
     FGB_CUDA(S::launch_sur_step(g->d_cloths, g->d_tiles, n_tiles, par, g->d_blob, g->norm, cst, g->groups, 0,
                                 g->d_err, st));
     if (checks) {
       FGB_CHECK_RC(run_check(g, s, n_tiles, par ^ 1, e_new, st));
-      bool any = false;
+      failing.clear();
       for (size_t c = 0; c < s->meshes.size(); ++c) {
-        const float E0 = e_old[c].x, E1 = e_new[c].x, S1 = e_new[c].y;
-        const bool ok = (E1 <= E0 + chk->energy_growth * std::fabs(E0) + chk->energy_abs) && (S1 <= chk->max_strain);
-        if (ok) continue;
-        any = true;
-        ++fallbacks;
-        fgb_mesh* m = s->meshes[c];
-        const fgb::GridTopo gt{int(m->topo.rows), int(m->topo.cols), m->d_grid, 0};
-        const fgb::StepConsts fc = fgb::detail::make_consts(s->cfg, s->d_faces, s->n_faces, m->d_flags, &s->accel);
-        int a = par;
-        for (uint32_t j = 0; j < ratio; ++j, a ^= 1)
-          FGB_CUDA(fgb::launch_step_grid(gt, static_cast<const float4*>(m->pos[a]), static_cast<const float4*>(m->vel[a]),
-                                         nullptr, static_cast<float4*>(m->pos[a ^ 1]),
-                                         static_cast<float4*>(m->vel[a ^ 1]), fc, st));
-        if (a != (par ^ 1)) {
-          const size_t bytes = size_t(m->topo.n) * sizeof(float4);
-          FGB_CUDA(cudaMemcpyAsync(m->pos[par ^ 1], m->pos[a], bytes, cudaMemcpyDeviceToDevice, st));
-          FGB_CUDA(cudaMemcpyAsync(m->vel[par ^ 1], m->vel[a], bytes, cudaMemcpyDeviceToDevice, st));
-        }
+        const double E0 = e_old[c].x, E1 = e_new[c].x, S1 = e_new[c].y;
+        const double margin = double(chk->energy_growth) * (std::fabs(E0) + e_ref[c]) + double(chk->energy_abs);
+        const bool ok = (E1 <= E0 + margin) && (S1 <= double(chk->max_strain));
+        if (!ok) failing.push_back(int(c));
       }
-      if (any) FGB_CHECK_RC(run_check(g, s, n_tiles, par ^ 1, e_new, st));
+      if (!failing.empty()) {
+        fallbacks += failing.size();
+        FGB_CHECK_RC(fine_fallback(g, s, failing, par, ratio, st));
+        FGB_CHECK_RC(run_check(g, s, n_tiles, par ^ 1, e_new, st));
+      }
       e_old.swap(e_new);
     }
     s->parity ^= 1;

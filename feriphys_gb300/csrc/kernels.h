@@ -55,7 +55,7 @@ struct ClothDesc {
   unsigned* flags;         // non-finite flag of this cloth
   int rows, cols;
   float wind[3];
-  int pad;
+  int skip;  // nonzero: the batched step leaves this cloth untouched (masked fallback steps)
 };
 
 // Tiles of one cloth for the batch work list: {cloth, tile x, tile y, interior}.

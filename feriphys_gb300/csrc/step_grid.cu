@@ -490,6 +490,10 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothD
     if (item >= n_work) break;
     const int4 w = work[item];
     const ClothDesc& d = cloths[w.x];
+    if (d.skip) {  // masked out: uniform over the CTA
+      if (!persistent) break;
+      continue;
+    }
     const V3<float> wind{d.wind[0], d.wind[1], d.wind[2]};
     if (w.w)
       tile_step<TW, TH, HALO, true>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,

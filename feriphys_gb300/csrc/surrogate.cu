@@ -43,20 +43,25 @@ __device__ __forceinline__ float2 unpack_bf2(uint32_t u) {
 }
 
 // GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its
-// slope, in this operation order.
+// slope 0.5 (1 + t) + 0.5 x (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 x^2), with
+// explicit fused multiply-adds (this file is compiled with -fmad=false).
 __device__ __forceinline__ float gelu(float x) {
   const float x2 = x * x;
-  const float u = kGeluC * (x + kGeluA * (x2 * x));
+  const float u = kGeluC * __fmaf_rn(kGeluA * x2, x, x);
   const float t = tc::tanh_fast(u);
-  return (0.5f * x) * (1.0f + t);
+  const float hx = 0.5f * x;
+  return __fmaf_rn(hx, t, hx);
 }
 
 __device__ __forceinline__ void gelu_slope(float x, float& g, float& dg) {
   const float x2 = x * x;
-  const float u = kGeluC * (x + kGeluA * (x2 * x));
+  const float u = kGeluC * __fmaf_rn(kGeluA * x2, x, x);
   const float t = tc::tanh_fast(u);
-  g = (0.5f * x) * (1.0f + t);
-  dg = 0.5f * (1.0f + t) + ((0.5f * x) * (1.0f - t * t)) * (kGeluC * (1.0f + (3.0f * kGeluA) * x2));
+  const float hx = 0.5f * x;
+  g = __fmaf_rn(hx, t, hx);
+  const float one_m_t2 = __fmaf_rn(-t, t, 1.0f);
+  const float du = kGeluC * __fmaf_rn(3.0f * kGeluA, x2, 1.0f);
+  dg = __fmaf_rn(hx * one_m_t2, du, __fmaf_rn(0.5f, t, 0.5f));
 }
 
 __device__ __forceinline__ void group_sync(int id) {
@@ -895,6 +900,16 @@ __global__ void k_check_reduce(const SurCloth* __restrict__ cloths, int n_cloths
   if (lane == 0) cloth_out[c] = make_float2(E, S);
 }
 
+__global__ void k_copy_unskipped(const ClothDesc* __restrict__ cloths, int from) {
+  const ClothDesc& d = cloths[blockIdx.x];
+  if (d.skip) return;
+  const int n = d.rows * d.cols;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d.pos[from ^ 1][i] = d.pos[from][i];
+    d.vel[from ^ 1][i] = d.vel[from][i];
+  }
+}
+
 int g_sms = 0;
 
 int sm_count() {
@@ -1031,6 +1046,12 @@ cudaError_t launch_check(const SurCloth* cloths, const Tile* tiles, int n_tiles,
   if (n_tiles <= 0) return cudaSuccess;
   k_check<<<n_tiles, kTile, 0, s>>>(cloths, tiles, n_tiles, parity, gforce, tile_out);
   k_check_reduce<<<(n_cloths * 32 + 255) / 256, 256, 0, s>>>(cloths, n_cloths, tile_out, cloth_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_unskipped(const ClothDesc* cloths, int n_cloths, int from, cudaStream_t s) {
+  if (n_cloths <= 0) return cudaSuccess;
+  k_copy_unskipped<<<n_cloths, 256, 0, s>>>(cloths, from);
   return cudaGetLastError();
 }
 

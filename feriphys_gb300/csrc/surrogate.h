@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "kernels.h"
 #include "step_consts.h"
 
 namespace fgb {
@@ -149,6 +150,11 @@ cudaError_t launch_stats(const float* feat, const float* tgt, long long count, d
 // tiles in a fixed order): cloth_out[c] = {E, strain}.
 cudaError_t launch_check(const SurCloth* cloths, const Tile* tiles, int n_tiles, int n_cloths, int parity,
                          float3 gforce, float2* tile_out, float2* cloth_out, cudaStream_t s);
+
+// For every cloth of a batched-step table whose skip flag is 0: copy its
+// state from buffers [from] to [from ^ 1] (the fine-step fallback restores
+// the pre-step state before stepping from it).
+cudaError_t launch_copy_unskipped(const ClothDesc* cloths, int n_cloths, int from, cudaStream_t s);
 
 }  // namespace sur
 }  // namespace fgb

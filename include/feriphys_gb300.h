@@ -278,11 +278,17 @@ int fgb_sim_destroy(fgb_sim* s);
  * T / h (T the coarse step, h the cloth's rest spacing). */
 typedef struct fgb_surrogate fgb_surrogate;
 
+/* Per-cloth check after every coarse step.  E = sum m|v|^2/2 - g.p + sum over
+ * struts k(|d| - L)^2/2 (g: the gravity force of a point), strain = the
+ * largest |(|d| - L) / L|.  A cloth fails when
+ *   E_new > E_old + energy_growth * (|E_old| + W h) + energy_abs
+ * (W h: the cloth's weight times its rest spacing, the energy of lifting it
+ * by one spacing) or when its strain exceeds max_strain. */
 typedef struct fgb_surrogate_check {
-  int32_t enabled;      /* 0: no checks, no fallback                                   */
-  float energy_growth;  /* fail when E_new > E_old + energy_growth * |E_old| + energy_abs */
-  float energy_abs;     /* J                                                             */
-  float max_strain;     /* fail when any strut's |(|d| - L) / L| exceeds this            */
+  int32_t enabled;      /* 0: no checks, no fallback */
+  float energy_growth;
+  float energy_abs;     /* J */
+  float max_strain;
 } fgb_surrogate_check;
 
 /* New network on the current device: Xavier-uniform weights from `seed`,

@@ -210,6 +210,24 @@ def test_fallback_reverts_to_fine_steps():
     assert np.array_equal(mesh.get_points(), mesh2.get_points())
 
 
+def test_batched_fallback_reverts_every_failing_cloth():
+    batch = W.c2(n_cloths=5, lo=12, hi=70, seed=3, dt=1.0 / 6000.0)
+    sim, meshes, _ = W.build_batch(batch, fgb)
+    sim2, meshes2, _ = W.build_batch(batch, fgb)
+    sur = fgb.Surrogate.new(14)
+    sur.set_normalization(np.zeros(54), np.ones(54), np.zeros(3), np.full(3, 100.0))
+    chk = fgb.SurrogateCheck.make(energy_growth=0.05, energy_abs=1e-6, max_strain=0.3)
+    assert sim.step_surrogate(sur, 10, 2, chk) == 10
+    sim2.step(20)
+    for a, b in zip(meshes, meshes2):
+        assert np.array_equal(a.get_points(), b.get_points())
+    # odd ratio: no restoring copy, the masked steps end in the other buffer directly
+    assert sim.step_surrogate(sur, 3, 1, chk) == 5
+    sim2.step(3)
+    for a, b in zip(meshes, meshes2):
+        assert np.array_equal(a.get_points(), b.get_points())
+
+
 def test_energy_matches_numpy():
     sc, sim, mesh, _ = small_scene()
     sim.step(20)
