@@ -118,6 +118,7 @@ def _declare(l):
         "fgb_config_default": (I, [cfg]),
         "fgb_mesh_new": (I, [P, U64, P, U64, F, F, F, P, U64, pp]),
         "fgb_cloth_new": (I, [U64, U64, F, P, F, F, F, F, F, F, F, P, U64, pp]),
+        "fgb_mesh_new_device": (I, [P, U64, P, U64, F, F, F, P, U64, pp]),
         "fgb_mesh_add_strut": (I, [P, U32, U32, F, F]),
         "fgb_mesh_add_pin": (I, [P, U32]),
         "fgb_mesh_add_struts": (I, [P, P, P, P, P, U64]),
@@ -130,6 +131,8 @@ def _declare(l):
         "fgb_mesh_get_positions": (I, [P, P]),
         "fgb_mesh_get_points_f64": (I, [P, P]),
         "fgb_mesh_get_vertices": (I, [P, P, P]),
+        "fgb_mesh_export_vertices": (I, [P, P, P, P]),
+        "fgb_mesh_export_indices": (I, [P, P, P]),
         "fgb_mesh_set_path": (I, [P, I]),
         "fgb_mesh_get_path": (I, [P, C.POINTER(C.c_int)]),
         "fgb_mesh_set_precision": (I, [P, I]),
@@ -221,9 +224,10 @@ class SpringyMesh:
 
     @classmethod
     def new(cls, vertex_positions, vertex_indices, mass, default_stiffness, default_damping,
-            strut_overrides=None) -> "SpringyMesh":
+            strut_overrides=None, build_on_device=False) -> "SpringyMesh":
         """SpringyMesh::new.  strut_overrides: {(a, b): (stiffness, damping)} or
-        a pair of arrays (pairs[n, 2], kc[n, 2]), or None."""
+        a pair of arrays (pairs[n, 2], kc[n, 2]), or None.  build_on_device:
+        de-duplicate the struts on the GPU (fgb_mesh_new_device, same mesh)."""
         pos = _f32(vertex_positions)
         idx = _u32(vertex_indices)
         ov = None
@@ -243,9 +247,9 @@ class SpringyMesh:
             rec[:, 0:2] = pairs
             rec[:, 2:4] = kc.view(np.uint32)
         h = C.c_void_p()
-        _check(_lib().fgb_mesh_new(_ptr(pos), pos.size // 3, _ptr(idx), idx.size, float(mass),
-                                   float(default_stiffness), float(default_damping),
-                                   C.cast(ov, C.c_void_p) if ov is not None else None, nov, C.byref(h)))
+        fn = _lib().fgb_mesh_new_device if build_on_device else _lib().fgb_mesh_new
+        _check(fn(_ptr(pos), pos.size // 3, _ptr(idx), idx.size, float(mass), float(default_stiffness),
+                  float(default_damping), C.cast(ov, C.c_void_p) if ov is not None else None, nov, C.byref(h)))
         return cls(h.value)
 
     def __del__(self):
@@ -318,6 +322,18 @@ class SpringyMesh:
         idx = np.empty(3 * f, np.uint32)
         _check(_lib().fgb_mesh_get_vertices(self._h, _ptr(pos), _ptr(idx)))
         return pos, idx
+
+    def export_vertices(self, device_ptr: int, color=None, stream_handle=None):
+        """Write ColoredVertex {position, color, normal} (9 f32 per vertex) into
+        a device buffer (e.g. ``tensor.data_ptr()`` of a CUDA tensor)."""
+        col = None if color is None else _f32(color)
+        _check(_lib().fgb_mesh_export_vertices(self._h, C.c_void_p(device_ptr), _ptr(col),
+                                               C.c_void_p(stream_handle) if stream_handle else None))
+
+    def export_indices(self, device_ptr: int, stream_handle=None):
+        """Write the static uint32 index buffer (3 per face) into a device buffer."""
+        _check(_lib().fgb_mesh_export_indices(self._h, C.c_void_p(device_ptr),
+                                              C.c_void_p(stream_handle) if stream_handle else None))
 
     def get_struts(self):
         """(kcl [S, 3]: stiffness, damping, rest length; ab [S, 2])."""

@@ -657,6 +657,26 @@ int fgb_mesh_new(const float* positions, uint64_t n_vertices, const uint32_t* in
   return finish_new_mesh(std::move(topo), out);
 }
 
+int fgb_mesh_new_device(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                        float mass, float default_stiffness, float default_damping,
+                        const fgb_spring_override* overrides, uint64_t n_overrides, fgb_mesh** out) {
+  if (!out) return fail(FGB_EINVAL, "null out");
+  *out = nullptr;
+  std::vector<fgb::Override> ov(n_overrides);
+  for (uint64_t i = 0; i < n_overrides; ++i)
+    ov[i] = fgb::Override{overrides[i].a, overrides[i].b, overrides[i].stiffness, overrides[i].damping};
+  MeshTopo topo;
+  std::string err;
+  try {
+    const int rc = fgb::build_springy_device(positions, n_vertices, indices, n_indices, mass, default_stiffness,
+                                             default_damping, ov.data(), n_overrides, topo, err);
+    if (rc) return fail(rc, err);
+  } catch (const std::bad_alloc&) {
+    return fail(FGB_ENOMEM, "out of host memory");
+  }
+  return finish_new_mesh(std::move(topo), out);
+}
+
 int fgb_cloth_new(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass,
                   float tensile_stiffness, float tensile_damping, float shear_stiffness, float shear_damping,
                   float binding_stiffness, float binding_damping, const uint32_t* pinned, uint64_t n_pinned,
@@ -834,6 +854,33 @@ int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices) {
   if (!m) return fail(FGB_EINVAL, "null mesh");
   if (positions) FGB_CHECK_RC(fgb_mesh_get_positions(m, positions));
   if (indices) std::memcpy(indices, m->topo.fv.data(), m->topo.fv.size() * sizeof(uint32_t));
+  return FGB_OK;
+}
+
+int fgb_mesh_export_vertices(fgb_mesh* m, void* device_out, const float* color, void* stream) {
+  if (!m || !device_out) return fail(FGB_EINVAL, "null argument");
+  FGB_CHECK_RC(ensure_device(m));
+  FGB_CHECK_RC(ensure_csr(m));
+  const cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : m->stream;
+  if (st != m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
+  const float r = color ? color[0] : 1.0f, g = color ? color[1] : 1.0f, b = color ? color[2] : 1.0f;
+  const int n = int(m->topo.n);
+  if (m->precision == 64)
+    FGB_CUDA(fgb::launch_render_vertices<double>(n, m->pos[m->cur], m->d_face_off, m->d_face_inc, m->d_face_vtx, r, g,
+                                                 b, static_cast<float*>(device_out), st));
+  else
+    FGB_CUDA(fgb::launch_render_vertices<float>(n, m->pos[m->cur], m->d_face_off, m->d_face_inc, m->d_face_vtx, r, g,
+                                                b, static_cast<float*>(device_out), st));
+  return FGB_OK;
+}
+
+int fgb_mesh_export_indices(fgb_mesh* m, void* device_out, void* stream) {
+  if (!m || !device_out) return fail(FGB_EINVAL, "null argument");
+  FGB_CHECK_RC(ensure_device(m));
+  const cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : m->stream;
+  FGB_CUDA(cudaMemcpyAsync(device_out, m->topo.fv.data(), m->topo.fv.size() * sizeof(uint32_t),
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
   return FGB_OK;
 }
 

@@ -135,6 +135,10 @@ void duration_parts(float x, uint64_t& secs, uint32_t& nanos) {
 
 }  // namespace
 
+bool detect_cloth_pattern(const uint32_t* idx, uint64_t nt, uint32_t n, uint32_t& R, uint32_t& C) {
+  return cloth_pattern(idx, nt, n, R, C);
+}
+
 float duration_roundtrip(float x) {
   uint64_t secs;
   uint32_t nanos;

@@ -41,6 +41,13 @@ int build_springy(const float* pos, uint64_t nv, const uint32_t* idx, uint64_t n
 int build_cloth(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass, float tk,
                 float tc, float sk, float sc, float bk, float bc, const uint32_t* pins, uint64_t npins,
                 MeshTopo& out, std::string& err);
+// The same result as build_springy with the strut de-duplication, the
+// face/strut adjacency and the strut constants computed on the current GPU
+// (mesh_build_gpu.cu); identical output, including error codes and messages.
+int build_springy_device(const float* pos, uint64_t nv, const uint32_t* idx, uint64_t ni, float mass, float k,
+                         float c, const Override* ov, uint64_t nov, MeshTopo& out, std::string& err);
+// True when the triangle list is exactly Cloth::new's for some rows x cols.
+bool detect_cloth_pattern(const uint32_t* idx, uint64_t nt, uint32_t n, uint32_t& R, uint32_t& C);
 // add_strut: rest length from the points' current positions, read at
 // cur_pos[stride * i + 0..2].
 int add_strut(MeshTopo& m, uint32_t a, uint32_t b, float k, float c, const float* cur_pos, size_t stride,

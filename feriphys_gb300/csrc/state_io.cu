@@ -58,6 +58,35 @@ __global__ void k_set_pins(int n, const uint8_t* __restrict__ pinned, Vec4<T>* _
 
 inline int nb(int n) { return (n + 255) / 256; }
 
+template <class T>
+__global__ void k_render_vertices(int n, const Vec4<T>* __restrict__ pos, const int* __restrict__ face_off,
+                                  const int* __restrict__ face_inc, const int4* __restrict__ face_vtx, float cr,
+                                  float cg, float cb, float* __restrict__ out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  V3<float> N{0.0f, 0.0f, 0.0f};
+  for (int k = face_off[v]; k < face_off[v + 1]; ++k) {
+    const int4 f = face_vtx[face_inc[k] >> 2];
+    const Vec4<T> A = pos[f.x], B = pos[f.y], C = pos[f.z];
+    const V3<float> a{float(A.x), float(A.y), float(A.z)};
+    const V3<float> e1 = a - V3<float>{float(B.x), float(B.y), float(B.z)};
+    const V3<float> e2 = a - V3<float>{float(C.x), float(C.y), float(C.z)};
+    N = N + cross(e1, e2);
+  }
+  N = normalize(N);
+  const Vec4<T> P = pos[v];
+  float* o = out + 9 * size_t(v);
+  o[0] = float(P.x);
+  o[1] = float(P.y);
+  o[2] = float(P.z);
+  o[3] = cr;
+  o[4] = cg;
+  o[5] = cb;
+  o[6] = N.x;
+  o[7] = N.y;
+  o[8] = N.z;
+}
+
 }  // namespace
 
 template <class T>
@@ -108,5 +137,19 @@ cudaError_t launch_set_pins(int n, const uint8_t* pinned, void* vel, cudaStream_
   template cudaError_t launch_set_pins<T>(int, const uint8_t*, void*, cudaStream_t);
 FGB_IO_INST(float)
 FGB_IO_INST(double)
+
+template <class T>
+cudaError_t launch_render_vertices(int n, const void* pos, const int* face_off, const int* face_inc,
+                                   const int4* face_vtx, float r, float g, float b, float* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_render_vertices<T><<<(n + 255) / 256, 256, 0, s>>>(n, static_cast<const Vec4<T>*>(pos), face_off, face_inc,
+                                                       face_vtx, r, g, b, out);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_render_vertices<float>(int, const void*, const int*, const int*, const int4*, float,
+                                                   float, float, float*, cudaStream_t);
+template cudaError_t launch_render_vertices<double>(int, const void*, const int*, const int*, const int4*, float,
+                                                    float, float, float*, cudaStream_t);
 
 }  // namespace fgb

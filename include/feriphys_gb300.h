@@ -87,6 +87,16 @@ int fgb_mesh_new(const float* positions, uint64_t n_vertices, const uint32_t* in
                  float mass, float default_stiffness, float default_damping,
                  const fgb_spring_override* overrides, uint64_t n_overrides, fgb_mesh** out);
 
+/* fgb_mesh_new with the strut de-duplication, the face/strut adjacency and
+ * the strut constants built on the current GPU (a radix sort of the edge
+ * keys instead of springy_mesh.rs:284-345's hash map) -- for meshes of
+ * millions of vertices.  Same arguments, same errors, and the same mesh bit
+ * for bit (strut order, constants, rest lengths, adjacency).  Extension with
+ * no reference counterpart. */
+int fgb_mesh_new_device(const float* positions, uint64_t n_vertices, const uint32_t* indices, uint64_t n_indices,
+                        float mass, float default_stiffness, float default_damping,
+                        const fgb_spring_override* overrides, uint64_t n_overrides, fgb_mesh** out);
+
 /* Cloth::new -- springy/cloth.rs:20-113 (rows, cols >= 2).  Builds the grid,
  * its triangles, the shear overrides, the pins and the binding struts. */
 int fgb_cloth_new(uint64_t rows, uint64_t cols, float spacing, const float position[3], float point_mass,
@@ -133,6 +143,21 @@ int fgb_mesh_get_points_f64(fgb_mesh* m, double* out);
 /* SpringyMesh::get_vertices -- springy_mesh.rs:500-513 (positions 3*N,
  * indices 3*F; either pointer may be NULL). */
 int fgb_mesh_get_vertices(fgb_mesh* m, float* positions, uint32_t* indices);
+
+/* Headless render export (replaces the per-frame host rebuild of
+ * ColoredMesh::from_springy_mesh, graphics/model.rs:72-90, 142-186).
+ * fgb_mesh_export_vertices writes, into the caller's DEVICE buffer of
+ * 9 * N floats, each vertex as ColoredVertex {position, color, normal}
+ * (model.rs:20-24) straight from the simulation's device state; the normal is
+ * graphics/util.rs:178-199's: the sum in face order of (p_a - p_b) x
+ * (p_a - p_c) over the vertex's faces, normalised.  color: 3 floats or NULL
+ * (white).  fgb_mesh_export_indices writes the static index buffer (3 * F
+ * uint32, so no 65,535-vertex cap as with the reference's u16 indices) into
+ * a device buffer once.  stream: a cudaStream_t or NULL for the mesh's own;
+ * the vertex export is asynchronous on it (ordered after the mesh's queued
+ * steps); the index export returns when the copy is done. */
+int fgb_mesh_export_vertices(fgb_mesh* m, void* device_out, const float* color, void* stream);
+int fgb_mesh_export_indices(fgb_mesh* m, void* device_out, void* stream);
 
 /* Select the step implementation: 0 = automatic (grid kernel when the mesh
  * is a Cloth::new grid, else the general gather), 1 = general gather,
