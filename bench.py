@@ -6,9 +6,13 @@ noise, top row pinned, wind, drag/lift, plane + UV-sphere colliders,
 explicit Euler at dt = 1/600 s) built by feriphys_gb300.workloads.c1 on
 synthetic seeded data.  A "step" is one Simulation::step of that cloth.
 Rollouts restart from the initial state every --rollout steps outside the
-timed region: 50 by default, because explicit Euler at the configured dt
-makes this cloth's state non-finite at step 62 (bench.py --probe), and every
-timed step should run on finite data.
+timed region: 30 by default.  Explicit Euler at the configured dt is
+unstable on this cloth: from step ~36 the largest speed doubles every two
+steps and the state is non-finite at step 62 (bench.py --probe); from step
+~45 the exploding vertices' segments cross the whole sphere, so the exact
+first-hit search tests every obstacle face for them and a step costs ~3.5x
+more.  Rollouts of 30 keep every timed step on the physical part of the
+trajectory (each one a complete step of the configuration).
 
 Timing: W warm-up steps, then K steps; L2 is flushed (a 256 MB write) before
 every timed step and each step is timed with CUDA events on the stream the
@@ -189,7 +193,7 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
     by default here) captured once as a CUDA graph and replayed; each rollout
     restarts from the initial state outside the timed region.  The working set
     (~3 GB) is far larger than L2, so no flush is needed."""
-    rollout = args.rollout if args.rollout != 50 else 100
+    rollout = args.rollout if args.rollout != 30 else 100
     t0 = time.perf_counter()
     batch = W.c2(n_cloths=args.cloths, seed=rank)
     sim, meshes, _ = W.build_batch(batch, fgb)
@@ -444,7 +448,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1024, help="cloth side in vertices")
-    ap.add_argument("--rollout", type=int, default=50)
+    ap.add_argument("--rollout", type=int, default=30)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -557,6 +561,7 @@ def main():
         dist.barrier()
     times = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)], np.float64)  # ms
     ms_step = float(times.mean())
+    ms_median = float(np.median(times))
     if dist:
         t = torch.tensor([ms_step], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -611,6 +616,7 @@ def main():
                            "l2": "flushed (256 MB write) before every timed step",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
+                "ms_per_step_median": ms_median,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": args.steps * kernels_per_step(mesh, args),
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
