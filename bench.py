@@ -293,6 +293,10 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     the energy/strain checks and per-cloth fine-step fallback) next to the
     fine solver over the same simulated time, from the same initial state."""
     ratio = args.ratio
+    if args.train_steps <= 0:
+        args.train_steps = 3000 if args.workload == "c3" else 8000
+    if args.collect_skip <= 0:
+        args.collect_skip = 60 if args.workload == "c3" else 30
     dt_f = args.fine_dt if args.fine_dt > 0 else 1.0 / 30000.0
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -300,7 +304,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     sur = fgb.Surrogate.new(1234 + rank)
     if args.workload == "c3":
         n = args.n
-        train_side = min(256, n)
+        train_side = min(args.train_side, n)
         ring = args.ring
         sur.reserve(ring)
         per_cloth = max(1, ring // (args.train_cloths * train_side * train_side))
@@ -461,10 +465,12 @@ def main():
     ap.add_argument("--ratio", type=int, default=10, help="fine steps per surrogate coarse step")
     ap.add_argument("--coarse-steps", type=int, default=1000)
     ap.add_argument("--fine-dt", type=float, default=0.0, help="fine step of the surrogate workloads (0: default)")
-    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--train-steps", type=int, default=0, help="Adam steps (0: c3 3000, c4 8000)")
     ap.add_argument("--train-cloths", type=int, default=4)
-    ap.add_argument("--ring", type=int, default=4 * 1024 * 1024, help="dataset ring rows")
-    ap.add_argument("--collect-skip", type=int, default=60, help="coarse steps between collected snapshots")
+    ap.add_argument("--train-side", type=int, default=256, help="c3: side of the training cloths")
+    ap.add_argument("--ring", type=int, default=16 * 1024 * 1024, help="dataset ring rows")
+    ap.add_argument("--collect-skip", type=int, default=0,
+                    help="coarse steps between collected snapshots (0: c3 60, c4 30)")
     ap.add_argument("--energy-growth", type=float, default=0.05)
     ap.add_argument("--max-strain", type=float, default=100.0)
     args = ap.parse_args()
