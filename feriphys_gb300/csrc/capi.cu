@@ -391,6 +391,7 @@ int prepare_batch(fgb_sim* s) {
     s->n_work = int(work.size() / 4);
     FGB_CUDA(dalloc(s->d_work, work.size() * sizeof(int)));
     FGB_CUDA(cudaMemcpy(s->d_work, work.data(), work.size() * sizeof(int), cudaMemcpyHostToDevice));
+    s->work_host = work;
     if (!s->d_counter) FGB_CUDA(dalloc(s->d_counter, sizeof(int)));
     drop_graphs(s);
     s->mode = -1;

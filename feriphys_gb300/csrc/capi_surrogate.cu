@@ -95,6 +95,9 @@ struct fgb_surrogate {
   size_t out_cap = 0;
   fgb::ClothDesc* d_fdesc = nullptr;  // batched fine-step fallback table (batch order, skip flags)
   size_t fdesc_cap = 0;
+  int4* d_fwork = nullptr;            // work items of the failing cloths only
+  size_t fwork_cap = 0;
+  int* d_fcounter = nullptr;
   int groups = 4;
 };
 
@@ -355,13 +358,23 @@ int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing,
   std::vector<char> fail_mesh(s->meshes.size(), 0);
   for (int c : failing) fail_mesh[c] = 1;
   std::vector<fgb::ClothDesc> d = s->desc;
+  std::vector<char> fail_batch(s->batch.size(), 0);
   for (size_t b = 0; b < s->batch.size(); ++b) {
     const size_t mi = size_t(std::find(s->meshes.begin(), s->meshes.end(), s->batch[b]) - s->meshes.begin());
-    d[b].skip = (mi < fail_mesh.size() && fail_mesh[mi]) ? 0 : 1;
+    fail_batch[b] = (mi < fail_mesh.size() && fail_mesh[mi]) ? 1 : 0;
+    d[b].skip = fail_batch[b] ? 0 : 1;
     d[b].force_in = nullptr;
   }
+  // the failing cloths' work items, in the list's order (largest cloths and boundary tiles first)
+  std::vector<int> fw;
+  for (size_t i = 0; i + 3 < s->work_host.size(); i += 4)
+    if (fail_batch[size_t(s->work_host[i])]) fw.insert(fw.end(), s->work_host.begin() + i, s->work_host.begin() + i + 4);
+  const int n_fw = int(fw.size() / 4);
   FGB_CUDA(dgrow(g->d_fdesc, g->fdesc_cap, d.size(), sizeof(fgb::ClothDesc)));
+  FGB_CUDA(dgrow(g->d_fwork, g->fwork_cap, std::max<size_t>(fw.size() / 4, 1), sizeof(int4)));
+  if (!g->d_fcounter) FGB_CUDA(cudaMalloc(&g->d_fcounter, sizeof(int)));
   FGB_CUDA(cudaMemcpyAsync(g->d_fdesc, d.data(), d.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice, st));
+  if (n_fw) FGB_CUDA(cudaMemcpyAsync(g->d_fwork, fw.data(), fw.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   int from = par;
   if ((ratio & 1u) == 0) {
     FGB_CUDA(S::launch_copy_unskipped(g->d_fdesc, int(d.size()), par, st));
@@ -374,9 +387,10 @@ int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     ctas = fgb::batched_ctas_per_sm() * sms;
   }
-  for (uint32_t j = 0; j < ratio; ++j) {
-    FGB_CUDA(cudaMemsetAsync(s->d_counter, 0, sizeof(int), st));
-    FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, s->d_work, s->n_work, s->d_counter, from ^ int(j & 1u), 1, ctas, fc,
+  ctas = std::max(1, std::min(ctas, n_fw));
+  for (uint32_t j = 0; j < ratio && n_fw > 0; ++j) {
+    FGB_CUDA(cudaMemsetAsync(g->d_fcounter, 0, sizeof(int), st));
+    FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, g->d_fwork, n_fw, g->d_fcounter, from ^ int(j & 1u), 1, ctas, fc,
                                       st));
   }
   FGB_CUDA(cudaStreamSynchronize(st));  // the host table must outlive its upload
@@ -461,6 +475,8 @@ int fgb_surrogate_destroy(fgb_surrogate* g) {
   dfree(g->d_cloth_chk);
   dfree(g->d_out);
   dfree(g->d_fdesc);
+  dfree(g->d_fwork);
+  dfree(g->d_fcounter);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
   return FGB_OK;

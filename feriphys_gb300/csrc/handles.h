@@ -102,6 +102,7 @@ struct fgb_sim {
   size_t d_desc_cap = 0;
   int4* d_work = nullptr;
   int n_work = 0;
+  std::vector<int> work_host;             // host copy of the work list (4 ints per item)
   int* d_counter = nullptr;
   int parity = 0;
   int mode = -1, ctas = 0;                // launch form chosen by the tuner
