@@ -294,9 +294,11 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     fine solver over the same simulated time, from the same initial state."""
     ratio = args.ratio
     if args.train_steps <= 0:
-        args.train_steps = 3000 if args.workload == "c3" else 8000
+        args.train_steps = 3000 if args.workload == "c3" else 20000
+    if args.ring <= 0:
+        args.ring = (16 if args.workload == "c3" else 32) * 1024 * 1024
     if args.collect_skip <= 0:
-        args.collect_skip = 60 if args.workload == "c3" else 30
+        args.collect_skip = 60 if args.workload == "c3" else max(1, args.coarse_steps // 20)
     dt_f = args.fine_dt if args.fine_dt > 0 else 1.0 / 30000.0
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -405,8 +407,11 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
             sur_ms += e0.elapsed_time(e1)
             done = c
             pts = [m.get_points() for m in smeshes]
-            per_cloth = [rollout_error(p, f) if np.isfinite(p).all() else float("inf") for p, f in zip(pts, refs[c])]
-            errors[c] = {"mean": float(np.mean(per_cloth)), "max": float(np.max(per_cloth))}
+            per_cloth = np.array([rollout_error(p, f) if np.isfinite(p).all() and np.isfinite(f).all() else np.nan
+                                  for p, f in zip(pts, refs[c])])
+            fin = per_cloth[np.isfinite(per_cloth)]
+            errors[c] = {"mean": float(fin.mean()) if fin.size else None, "max": float(fin.max()) if fin.size else None,
+                         "nonfinite_cloths": int((~np.isfinite(per_cloth)).sum())}
     coarse_ms = sur_ms / args.coarse_steps
     T = ratio * np.float32(dt_f)
     value = world * n_vert * ratio / (coarse_ms * 1e-3)
@@ -465,12 +470,13 @@ def main():
     ap.add_argument("--ratio", type=int, default=10, help="fine steps per surrogate coarse step")
     ap.add_argument("--coarse-steps", type=int, default=1000)
     ap.add_argument("--fine-dt", type=float, default=0.0, help="fine step of the surrogate workloads (0: default)")
-    ap.add_argument("--train-steps", type=int, default=0, help="Adam steps (0: c3 3000, c4 8000)")
+    ap.add_argument("--train-steps", type=int, default=0, help="Adam steps (0: c3 3000, c4 20000)")
     ap.add_argument("--train-cloths", type=int, default=4)
     ap.add_argument("--train-side", type=int, default=256, help="c3: side of the training cloths")
-    ap.add_argument("--ring", type=int, default=16 * 1024 * 1024, help="dataset ring rows")
+    ap.add_argument("--ring", type=int, default=0, help="dataset ring rows (0: c3 16M, c4 32M)")
     ap.add_argument("--collect-skip", type=int, default=0,
-                    help="coarse steps between collected snapshots (0: c3 60, c4 30)")
+                    help="coarse steps between collected snapshots (0: c3 60; c4 coarse-steps/20, so that the "
+                         "snapshots span the evaluated horizon)")
     ap.add_argument("--energy-growth", type=float, default=0.05)
     ap.add_argument("--max-strain", type=float, default=100.0)
     args = ap.parse_args()

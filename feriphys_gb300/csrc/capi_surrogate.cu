@@ -753,7 +753,8 @@ int fgb_sim_step_surrogate(fgb_sim* s, fgb_surrogate* g, uint32_t ratio, uint64_
       for (size_t c = 0; c < s->meshes.size(); ++c) {
         const double E0 = e_old[c].x, E1 = e_new[c].x, S1 = e_new[c].y;
         const double margin = double(chk->energy_growth) * (std::fabs(E0) + e_ref[c]) + double(chk->energy_abs);
-        const bool ok = (E1 <= E0 + margin) && (S1 <= double(chk->max_strain));
+        const bool ok = std::isfinite(E1) && std::isfinite(S1) && (E1 <= E0 + margin) &&
+                        (S1 <= double(chk->max_strain));
         if (!ok) failing.push_back(int(c));
       }
       if (!failing.empty()) {

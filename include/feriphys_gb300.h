@@ -308,7 +308,8 @@ typedef struct fgb_surrogate fgb_surrogate;
  * largest |(|d| - L) / L|.  A cloth fails when
  *   E_new > E_old + energy_growth * (|E_old| + W h) + energy_abs
  * (W h: the cloth's weight times its rest spacing, the energy of lifting it
- * by one spacing) or when its strain exceeds max_strain. */
+ * by one spacing), when its strain exceeds max_strain, or when either is not
+ * finite. */
 typedef struct fgb_surrogate_check {
   int32_t enabled;      /* 0: no checks, no fallback */
   float energy_growth;
