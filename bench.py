@@ -407,11 +407,14 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
             sur_ms += e0.elapsed_time(e1)
             done = c
             pts = [m.get_points() for m in smeshes]
-            per_cloth = np.array([rollout_error(p, f) if np.isfinite(p).all() and np.isfinite(f).all() else np.nan
-                                  for p, f in zip(pts, refs[c])])
+            ref_ok = np.array([np.isfinite(f).all() for f in refs[c]])
+            sur_ok = np.array([np.isfinite(p).all() for p in pts])
+            per_cloth = np.array([rollout_error(p, f) if a and b else np.nan
+                                  for p, f, a, b in zip(pts, refs[c], sur_ok, ref_ok)])
             fin = per_cloth[np.isfinite(per_cloth)]
             errors[c] = {"mean": float(fin.mean()) if fin.size else None, "max": float(fin.max()) if fin.size else None,
-                         "nonfinite_cloths": int((~np.isfinite(per_cloth)).sum())}
+                         "median": float(np.median(fin)) if fin.size else None,
+                         "nonfinite_fine": int((~ref_ok).sum()), "nonfinite_surrogate": int((~sur_ok).sum())}
     coarse_ms = sur_ms / args.coarse_steps
     T = ratio * np.float32(dt_f)
     value = world * n_vert * ratio / (coarse_ms * 1e-3)
@@ -439,7 +442,8 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                          "frac": achieved / peak, "traffic": None,
                          "algorithmic_flops_per_launch": SURROGATE_FLOPS_PER_VERTEX * n_vert,
                          "kernel_ms": kernel_ms,
-                         "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch"},
+                         "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch; "
+                                 "tensor-pipe utilisation from ncu in profiles/surrogate_step_c3.md"},
             "training": {"rows": rows, "collect_and_setup_s": collect_s, "steps": int(args.train_steps),
                          "batch": 65536, "seconds": train_s, "samples_per_s": args.train_steps * 65536 / train_s,
                          "loss_first": float(losses[0]), "loss_last": float(losses[-1])},

@@ -306,10 +306,11 @@ typedef struct fgb_surrogate fgb_surrogate;
 /* Per-cloth check after every coarse step.  E = sum m|v|^2/2 - g.p + sum over
  * struts k(|d| - L)^2/2 (g: the gravity force of a point), strain = the
  * largest |(|d| - L) / L|.  A cloth fails when
- *   E_new > E_old + energy_growth * (|E_old| + W h) + energy_abs
- * (W h: the cloth's weight times its rest spacing, the energy of lifting it
- * by one spacing), when its strain exceeds max_strain, or when either is not
- * finite. */
+ *   E_new > E_old + energy_growth * (|E_start| + W h) + energy_abs
+ * (E_start: the cloth's energy when the call began; W h: its weight times its
+ * rest spacing, the energy of lifting it by one spacing -- a scale fixed for
+ * the call, so the allowed growth adds up linearly, never geometrically),
+ * when its strain exceeds max_strain, or when either is not finite. */
 typedef struct fgb_surrogate_check {
   int32_t enabled;      /* 0: no checks, no fallback */
   float energy_growth;
