@@ -94,6 +94,19 @@ int ensure_stream(fgb_mesh* m) {
   return FGB_OK;
 }
 
+// Device address of a pinned (page-locked, mapped) host buffer, or null for
+// pageable memory, which is staged through a device buffer instead.
+template <class P>
+P* mapped_host(P* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return static_cast<P*>(a.devicePointer);
+}
+
 int ensure_io(fgb_mesh* m, size_t bytes) {
   if (m->d_io_bytes < bytes) {
     FGB_CUDA(dalloc(m->d_io, bytes));
@@ -775,8 +788,17 @@ int fgb_mesh_get_points(fgb_mesh* m, float* out) {
     return FGB_OK;
   }
   FGB_CUDA(cudaSetDevice(m->device));
-  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
   const void* F = m->has_force ? m->force : nullptr;
+  if (float* direct = mapped_host(out)) {
+    // pinned host rows: the conversion kernel writes them across the host link itself
+    if (m->precision == 64)
+      FGB_CUDA((fgb::launch_pack_f32<double>(int(n), m->pos[m->cur], m->vel[m->cur], F, direct, m->stream)));
+    else
+      FGB_CUDA((fgb::launch_pack_f32<float>(int(n), m->pos[m->cur], m->vel[m->cur], F, direct, m->stream)));
+    FGB_CUDA(cudaStreamSynchronize(m->stream));
+    return FGB_OK;
+  }
+  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
   if (m->precision == 64)
     FGB_CUDA((fgb::launch_pack_f32<double>(int(n), m->pos[m->cur], m->vel[m->cur], F, m->d_io, m->stream)));
   else
@@ -817,14 +839,18 @@ int fgb_mesh_set_points(fgb_mesh* m, const float* in) {
   // Device-resident: DMA the raw points and convert on the device; the
   // accumulated forces go to the force buffer (read once by the next step).
   FGB_CUDA(cudaSetDevice(m->device));
-  FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
   if (!m->force) FGB_CUDA(dalloc(m->force, m->elem() * n));
-  FGB_CUDA(cudaMemcpyAsync(m->d_io, in, 10 * sizeof(float) * n, cudaMemcpyHostToDevice, m->stream));
+  const float* rows = mapped_host(in);  // pinned host rows are read across the host link by the kernel itself
+  if (!rows) {
+    FGB_CHECK_RC(ensure_io(m, 10 * sizeof(float) * n));
+    FGB_CUDA(cudaMemcpyAsync(m->d_io, in, 10 * sizeof(float) * n, cudaMemcpyHostToDevice, m->stream));
+    rows = m->d_io;
+  }
   if (m->precision == 64)
-    FGB_CUDA((fgb::launch_unpack<double>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
+    FGB_CUDA((fgb::launch_unpack<double>(int(n), rows, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
                                          m->stream)));
   else
-    FGB_CUDA((fgb::launch_unpack<float>(int(n), m->d_io, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
+    FGB_CUDA((fgb::launch_unpack<float>(int(n), rows, m->d_pinned, m->pos[m->cur], m->vel[m->cur], m->force,
                                         m->stream)));
   FGB_CUDA(cudaStreamSynchronize(m->stream));
   m->has_force = true;

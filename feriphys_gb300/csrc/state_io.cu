@@ -58,6 +58,60 @@ __global__ void k_set_pins(int n, const uint8_t* __restrict__ pinned, Vec4<T>* _
 
 inline int nb(int n) { return (n + 255) / 256; }
 
+// The same conversions for f32 state with the Stateful rows moved as
+// coalesced 16-byte chunks through shared memory (256 points = 10 KB per
+// block); the rows may sit in device memory or, mapped, in pinned host memory,
+// which the kernel then reads or writes across the host link directly.  The
+// row pointer must be 16-byte aligned.
+constexpr int kIoBlock = 256;
+
+__global__ void __launch_bounds__(kIoBlock) k_unpack_staged(int n, const float* __restrict__ pts,
+                                                            const uint8_t* __restrict__ pinned,
+                                                            float4* __restrict__ pos, float4* __restrict__ vel,
+                                                            float4* __restrict__ force) {
+  __shared__ __align__(16) float buf[10 * kIoBlock];
+  const int first = blockIdx.x * kIoBlock;
+  const int cnt = min(kIoBlock, n - first);
+  const int nf = 10 * cnt;
+  const float* src = pts + 10 * size_t(first);
+  for (int k = threadIdx.x; k < nf / 4; k += kIoBlock)
+    reinterpret_cast<float4*>(buf)[k] = reinterpret_cast<const float4*>(src)[k];
+  for (int k = (nf / 4) * 4 + threadIdx.x; k < nf; k += kIoBlock) buf[k] = src[k];
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= cnt) return;
+  const float* p = buf + 10 * t;
+  const int i = first + t;
+  pos[i] = make_float4(p[1], p[2], p[3], p[0]);
+  vel[i] = make_float4(p[4], p[5], p[6], pinned[i] ? 1.0f : 0.0f);
+  if (force) force[i] = make_float4(p[7], p[8], p[9], 0.0f);
+}
+
+__global__ void __launch_bounds__(kIoBlock) k_pack_staged(int n, const float4* __restrict__ pos,
+                                                          const float4* __restrict__ vel,
+                                                          const float4* __restrict__ force, float* __restrict__ pts) {
+  __shared__ __align__(16) float buf[10 * kIoBlock];
+  const int first = blockIdx.x * kIoBlock;
+  const int cnt = min(kIoBlock, n - first);
+  const int t = threadIdx.x;
+  if (t < cnt) {
+    const int i = first + t;
+    const float4 P = pos[i], V = vel[i];
+    const float4 F = force ? force[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float* o = buf + 10 * t;
+    o[0] = P.w;
+    o[1] = P.x; o[2] = P.y; o[3] = P.z;
+    o[4] = V.x; o[5] = V.y; o[6] = V.z;
+    o[7] = F.x; o[8] = F.y; o[9] = F.z;
+  }
+  __syncthreads();
+  const int nf = 10 * cnt;
+  float* dst = pts + 10 * size_t(first);
+  for (int k = t; k < nf / 4; k += kIoBlock)
+    reinterpret_cast<float4*>(dst)[k] = reinterpret_cast<const float4*>(buf)[k];
+  for (int k = (nf / 4) * 4 + t; k < nf; k += kIoBlock) dst[k] = buf[k];
+}
+
 template <class T>
 __global__ void k_render_vertices(int n, const Vec4<T>* __restrict__ pos, const int* __restrict__ face_off,
                                   const int* __restrict__ face_inc, const int4* __restrict__ face_vtx, float cr,
@@ -93,6 +147,11 @@ template <class T>
 cudaError_t launch_unpack(int n, const float* pts, const uint8_t* pinned, void* pos, void* vel, void* force,
                           cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(pts) & 15) == 0) {
+    k_unpack_staged<<<(n + kIoBlock - 1) / kIoBlock, kIoBlock, 0, s>>>(
+        n, pts, pinned, static_cast<float4*>(pos), static_cast<float4*>(vel), static_cast<float4*>(force));
+    return cudaGetLastError();
+  }
   k_unpack<T><<<nb(n), 256, 0, s>>>(n, pts, pinned, static_cast<Vec4<T>*>(pos), static_cast<Vec4<T>*>(vel),
                                     static_cast<Vec4<T>*>(force));
   return cudaGetLastError();
@@ -101,6 +160,11 @@ cudaError_t launch_unpack(int n, const float* pts, const uint8_t* pinned, void* 
 template <class T>
 cudaError_t launch_pack_f32(int n, const void* pos, const void* vel, const void* force, float* pts, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(pts) & 15) == 0) {
+    k_pack_staged<<<(n + kIoBlock - 1) / kIoBlock, kIoBlock, 0, s>>>(
+        n, static_cast<const float4*>(pos), static_cast<const float4*>(vel), static_cast<const float4*>(force), pts);
+    return cudaGetLastError();
+  }
   k_pack<T, float><<<nb(n), 256, 0, s>>>(n, static_cast<const Vec4<T>*>(pos), static_cast<const Vec4<T>*>(vel),
                                           static_cast<const Vec4<T>*>(force), pts);
   return cudaGetLastError();
