@@ -460,7 +460,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=1024, help="cloth side in vertices")
+    ap.add_argument("--n", "--side", dest="n", type=int, default=1024, help="cloth side in vertices")
     ap.add_argument("--rollout", type=int, default=30)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
