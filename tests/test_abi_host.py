@@ -164,3 +164,38 @@ def test_points_round_trip_host(fgb):
     p[:, 4:10] = np.arange(18, dtype=np.float32).reshape(3, 6)
     m.set_points(p)
     assert (m.get_points() == p).all()
+
+
+def test_extension_entry_points_reject_bad_arguments(fgb):
+    """The surrogate, export and static-step entry points validate their
+    arguments on the host before touching a device."""
+    lib = fgb._lib()
+    null = None
+    f = (C.c_float * 64)()
+    u = (C.c_uint64 * 2)()
+    assert lib.fgb_surrogate_new(0, null) == -1
+    assert lib.fgb_surrogate_get_params(null, f) == -1
+    assert lib.fgb_surrogate_set_params(null, f) == -1
+    assert lib.fgb_surrogate_set_normalization(null, f, f, f, f) == -1
+    assert lib.fgb_surrogate_get_normalization(null, f, f, f, f) == -1
+    assert lib.fgb_surrogate_forward(null, f, 1, f) == -1
+    assert lib.fgb_surrogate_gradients(null, f, f, 128, f, null) == -1
+    assert lib.fgb_surrogate_train_batch(null, f, f, 128, C.c_float(1e-3), null) == -1
+    assert lib.fgb_surrogate_dataset_reserve(null, 10) == -1
+    assert lib.fgb_surrogate_collect(null, null, 10, 1) == -1
+    assert lib.fgb_surrogate_dataset_info(null, u) == -1
+    assert lib.fgb_surrogate_fit_normalization(null) == -1
+    assert lib.fgb_surrogate_train(null, 1, 128, C.c_float(1e-3), 0, null) == -1
+    assert lib.fgb_sim_step_surrogate(null, null, 10, 1, null, null) == -1
+    assert lib.fgb_sim_energy(null, f) == -1
+    assert lib.fgb_mesh_export_vertices(null, f, null, null) == -1
+    assert lib.fgb_mesh_export_indices(null, f, null) == -1
+    assert lib.fgb_surrogate_destroy(null) == 0
+    assert "null" in lib.fgb_last_error().decode()
+
+
+def test_device_build_rejects_bad_input_before_the_gpu(fgb):
+    pos = np.zeros((4, 3), np.float32)
+    with pytest.raises(fgb.FgbError) as e:
+        fgb.SpringyMesh.new(pos, np.array([0, 1, 7], np.uint32), 1.0, 1.0, 1.0, build_on_device=True)
+    assert e.value.code == -2 and "out of range" in str(e.value)
