@@ -408,11 +408,13 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
       take(KBH, lr, lc, 0);      // BH_RIGHT
       take(KBV, lr, lc, 0);      // BV_DOWN
     } else {
+#pragma unroll  // every slot but the last column's permuted three folds to constants
       for (int j = 0; j < N_SLOTS; ++j) {
         const SlotDesc d = slot_desc(slot_at(j, r, cc, R, C));
         if (owned_exists(d.kind, r + d.dr, cc + d.dc, R, C)) take(d.kind, lr + d.dr, lc + d.dc, d.role);
       }
     }
+#pragma unroll
     for (int sl = 0; sl < N_FACE_SLOTS; ++sl) {
       const FaceDesc fd = face_desc(sl);
       if (!INTERIOR && !quad_exists(r + fd.dr, cc + fd.dc, R, C)) continue;
