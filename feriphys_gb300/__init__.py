@@ -13,6 +13,13 @@ sm_103a).  Names follow the reference (file:line relative to its root):
                          get_meshes, get_obstacles, set_config)
     Config, Integration  springy/config.rs:9-33, state.rs:4-8
 
+Extensions with no reference counterpart: per-mesh wind and batched
+stepping controls on Simulation, Simulation.step_static (no allocation after
+set-up), SpringyMesh.new(..., build_on_device=True) (strut de-dup on the GPU),
+SpringyMesh.export_vertices / export_indices (render buffers written into
+device memory), and the learned surrogate (Surrogate, SurrogateCheck,
+Simulation.step_surrogate, Simulation.energy).
+
 There is no CPU fallback: importing the package loads the CUDA library (it is
 built first when missing or stale and nvcc is available) and raises if it
 cannot.

@@ -363,7 +363,10 @@ int fgb_surrogate_train(fgb_surrogate* g, uint64_t n_steps, uint64_t batch, floa
  * collision response against the obstacles over T, pinned vertices
  * unchanged.  With chk->enabled, a cloth whose energy or strain check fails
  * after a coarse step is reverted and advanced by `ratio` fine steps instead;
- * *n_fallbacks (may be NULL) receives the number of such reverts. */
+ * *n_fallbacks (may be NULL) receives the number of such reverts.  An
+ * accumulated force carried in by fgb_mesh_set_points does not enter a
+ * coarse step (the network sees positions and velocities only) and is
+ * cleared by it, as Simulation::step's clear_forces would. */
 int fgb_sim_step_surrogate(fgb_sim* s, fgb_surrogate* g, uint32_t ratio, uint64_t n_coarse,
                            const fgb_surrogate_check* chk, uint64_t* n_fallbacks);
 /* Energy and maximum strain of each mesh's current state (out[2 * n_meshes]),
