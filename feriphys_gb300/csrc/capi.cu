@@ -136,6 +136,7 @@ void free_topology(fgb_mesh* m) {
   dfree(m->d_face_inc);
   dfree(m->d_face_vtx);
   dfree(m->d_grid);
+  dfree(m->d_rest);
   m->csr_ready = false;
 }
 

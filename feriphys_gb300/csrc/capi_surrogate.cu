@@ -239,6 +239,18 @@ float mesh_spacing(fgb_mesh* m) {
   return m->rest_spacing;
 }
 
+// The positions the mesh was built from, on the device (x, y, z, 0).
+int ensure_rest(fgb_mesh* m) {
+  if (m->d_rest) return FGB_OK;
+  const size_t n = m->topo.n;
+  std::vector<float4> h(n);
+  for (size_t i = 0; i < n; ++i)
+    h[i] = make_float4(m->topo.pos[3 * i], m->topo.pos[3 * i + 1], m->topo.pos[3 * i + 2], 0.0f);
+  FGB_CUDA(cudaMalloc(&m->d_rest, std::max<size_t>(n, 1) * sizeof(float4)));
+  FGB_CUDA(cudaMemcpy(m->d_rest, h.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  return FGB_OK;
+}
+
 S::SurCloth make_cloth(fgb_mesh* m, float T, const float wind[3], long long vbase) {
   S::SurCloth c;
   std::memset(&c, 0, sizeof(c));
@@ -247,6 +259,7 @@ S::SurCloth make_cloth(fgb_mesh* m, float T, const float wind[3], long long vbas
     c.vel[k] = static_cast<float4*>(m->vel[k]);
   }
   c.planes = m->d_grid;
+  c.rest = m->d_rest;
   c.flags = m->d_flags;
   c.rows = int(m->topo.rows);
   c.cols = int(m->topo.cols);
@@ -307,6 +320,7 @@ int build_sim_tables(fgb_surrogate* g, fgb_sim* s, float T, long long vbase0, st
   cl.clear();
   tiles.clear();
   long long vb = vbase0;
+  for (fgb_mesh* m : s->meshes) FGB_CHECK_RC(ensure_rest(m));
   for (size_t i = 0; i < s->meshes.size(); ++i) {
     float w[3];
     mesh_wind(s, s->meshes[i], w);
@@ -536,6 +550,7 @@ int fgb_surrogate_features(fgb_surrogate* g, fgb_mesh* m, float coarse_dt, const
   if (!(coarse_dt > 0.0f) || !std::isfinite(coarse_dt)) return fail(FGB_EINVAL, "coarse_dt must be positive");
   FGB_CHECK_RC(fgb::detail::ensure_device(m));
   if (m->active_path != 2 || m->precision != 32) return fail(FGB_EINVAL, "features need a grid mesh (f32 grid path)");
+  FGB_CHECK_RC(ensure_rest(m));
   float w[3] = {0.0f, 0.0f, 0.0f};
   for (int k = 0; k < 3; ++k) w[k] = wind ? wind[k] : (m->has_wind ? m->wind[k] : 0.0f);
   std::vector<S::SurCloth> cl{make_cloth(m, coarse_dt, w, 0)};

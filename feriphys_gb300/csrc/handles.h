@@ -80,6 +80,7 @@ struct fgb_mesh {
   int4* d_face_vtx = nullptr;
   // grid topology
   float4* d_grid = nullptr;
+  float4* d_rest = nullptr;  // construction positions (x, y, z, 0), uploaded for the surrogate's inputs
 
   size_t elem() const { return precision == 64 ? sizeof(fgb::Dbl4) : sizeof(float4); }
 };

@@ -98,8 +98,9 @@ __device__ __forceinline__ void vertex_features(const SurCloth& c, int parity, i
   const int R = c.rows, C = c.cols;
   const float4* __restrict__ P = c.pos[parity];
   const float4* __restrict__ Vl = c.vel[parity];
+  const float4* __restrict__ P0 = c.rest;
   const int i = r * C + col;
-  const float4 p = P[i], v = Vl[i];
+  const float4 p = P[i], v = Vl[i], p0 = P0[i];
   const float ih = c.inv_h, s = c.sv;
   float3 q[8];
   bool has[8];
@@ -111,11 +112,11 @@ __device__ __forceinline__ void vertex_features(const SurCloth& c, int parity, i
     has[k] = rr >= 0 && rr < R && cc >= 0 && cc < C;
     if (has[k]) {
       const int j = rr * C + cc;
-      const float4 a = P[j], w = Vl[j];
+      const float4 a = P[j], w = Vl[j], a0 = P0[j];
       q[k] = make_float3(a.x, a.y, a.z);
-      f[3 * k + 0] = (a.x - p.x) * ih;
-      f[3 * k + 1] = (a.y - p.y) * ih;
-      f[3 * k + 2] = (a.z - p.z) * ih;
+      f[3 * k + 0] = ((a.x - p.x) - (a0.x - p0.x)) * ih;
+      f[3 * k + 1] = ((a.y - p.y) - (a0.y - p0.y)) * ih;
+      f[3 * k + 2] = ((a.z - p.z) - (a0.z - p0.z)) * ih;
       f[24 + 3 * k + 0] = (w.x - v.x) * s;
       f[24 + 3 * k + 1] = (w.y - v.y) * s;
       f[24 + 3 * k + 2] = (w.z - v.z) * s;

@@ -5,8 +5,9 @@
 //
 // Inputs of vertex (r, c) of a Cloth::new grid with rest spacing h, coarse
 // step T = ratio * dt, s = T / h (in this order; a missing neighbour gives
-// zeros):
-//   0..23   (p_nb - p) / h        for the 8 neighbours (dr, dc) =
+// zeros; p0 are the positions the mesh was built from, so the first block is
+// the stencil's deformation from its rest shape):
+//   0..23   ((p_nb - p) - (p0_nb - p0)) / h   for the 8 neighbours (dr, dc) =
 //           (-1,-1) (-1,0) (-1,1) (0,-1) (0,1) (1,-1) (1,0) (1,1)
 //   24..47  (v_nb - v) * s        same order
 //   48      pinned (1 or 0)
@@ -73,6 +74,7 @@ struct SurCloth {
   float4* pos[2];
   float4* vel[2];
   const float4* planes;  // owned-strut constants (grid_order.h), for the checks
+  const float4* rest;    // positions the mesh was built from (x, y, z, 0)
   unsigned* flags;       // bit 0: a vertex went non-finite
   int rows, cols;
   int tile0, ntiles;     // this cloth's tiles in the work list

@@ -288,8 +288,9 @@ int fgb_sim_destroy(fgb_sim* s);
  * A per-vertex MLP 54 -> 128 -> 128 -> 3 (tanh-form GELU, bf16 weights, f32
  * accumulation on the tensor cores) that predicts, for a vertex of a
  * Cloth::new grid, its velocity change over one coarse step of `ratio` fine
- * steps of the simulation's dt, from its 8-neighbour stencil (relative
- * positions and velocities), pin flag, relative wind and normal.  Training
+ * steps of the simulation's dt, from its 8-neighbour stencil (the
+ * neighbours' positions relative to the vertex, minus the same at rest, and
+ * relative velocities), pin flag, relative wind and normal.  Training
  * data comes from the simulation's own fine steps on the GPU; training
  * (forward, backward, Adam) and inference are CUDA kernels of this library.
  * The fine step stays the judge: fgb_sim_step_surrogate checks each cloth's

@@ -164,13 +164,16 @@ def spacing(construction_positions, rows, cols):
     return np.float32(np.sqrt((d ** 2).sum(-1)).mean())
 
 
-def features(pos, vel, rows, cols, h, T, wind):
+def features(pos, vel, rows, cols, h, T, wind, rest):
     """Raw inputs [n,54] of every vertex (f32, the GPU's operation order).
 
-    pos[n,4] = (x, y, z, mass), vel[n,4] = (vx, vy, vz, pinned)."""
+    pos[n,4] = (x, y, z, mass), vel[n,4] = (vx, vy, vz, pinned), rest[n,3] =
+    the positions the mesh was built from (the first 24 inputs are the
+    stencil's deformation from its rest shape)."""
     f32 = np.float32
     P = np.asarray(pos, f32).reshape(rows, cols, 4)
     V = np.asarray(vel, f32).reshape(rows, cols, 4)
+    P0 = np.asarray(rest, f32).reshape(rows, cols, 3)
     ih = f32(1) / f32(h)
     s = f32(T) / f32(h)
     out = np.zeros((rows, cols, N_FEAT), f32)
@@ -178,14 +181,16 @@ def features(pos, vel, rows, cols, h, T, wind):
     for k, (dr, dc) in enumerate(NEIGHBOURS):
         Pn = P[:, :, :3].copy()
         Vn = V[:, :, :3].copy()
+        Rn = P0.copy()
         has = np.zeros((rows, cols), bool)
         r0, r1 = max(0, -dr), rows - max(0, dr)
         c0, c1 = max(0, -dc), cols - max(0, dc)
         Pn[r0:r1, c0:c1] = P[r0 + dr:r1 + dr, c0 + dc:c1 + dc, :3]
         Vn[r0:r1, c0:c1] = V[r0 + dr:r1 + dr, c0 + dc:c1 + dc, :3]
+        Rn[r0:r1, c0:c1] = P0[r0 + dr:r1 + dr, c0 + dc:c1 + dc]
         has[r0:r1, c0:c1] = True
         q[k] = Pn
-        rel_p = (Pn - P[:, :, :3]) * ih
+        rel_p = ((Pn - P[:, :, :3]) - (Rn - P0)) * ih
         rel_v = (Vn - V[:, :, :3]) * s
         out[:, :, 3 * k:3 * k + 3] = np.where(has[..., None], rel_p, f32(0))
         out[:, :, 24 + 3 * k:24 + 3 * k + 3] = np.where(has[..., None], rel_v, f32(0))
@@ -210,14 +215,14 @@ def features(pos, vel, rows, cols, h, T, wind):
     return out.reshape(rows * cols, N_FEAT)
 
 
-def coarse_step(pos, vel, rows, cols, h, T, wind, params, in_mean, in_std, out_mean, out_std):
+def coarse_step(pos, vel, rows, cols, h, T, wind, rest, params, in_mean, in_std, out_mean, out_std):
     """One surrogate coarse step without obstacles: v' = v + dv,
     p' = p + (v + v') T / 2,
     pinned vertices unchanged.  Returns (pos', vel') as [n,4] f32."""
     f32 = np.float32
     P = np.asarray(pos, f32).reshape(-1, 4)
     V = np.asarray(vel, f32).reshape(-1, 4)
-    x = features(P, V, rows, cols, h, T, wind)
+    x = features(P, V, rows, cols, h, T, wind, rest)
     inv_std = f32(1) / np.asarray(in_std, f32)
     xn = (x - np.asarray(in_mean, f32)) * inv_std
     y = forward(params, xn)

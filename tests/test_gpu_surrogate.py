@@ -72,7 +72,7 @@ def test_features_match_oracle():
     got = sur.features(mesh, T, wind)
     pos, vel = cloth_state(mesh, pins)
     h = SO.spacing(W.grid_positions(rows, cols, s), rows, cols)
-    ref = SO.features(pos, vel, rows, cols, h, np.float32(T), wind)
+    ref = SO.features(pos, vel, rows, cols, h, np.float32(T), wind, W.grid_positions(rows, cols, s))
     assert np.all(np.abs(got[:, :52] - ref[:, :52]) <= 1e-6 * np.maximum(1.0, np.abs(ref[:, :52])))
     assert np.abs(got[:, 52:] - ref[:, 52:]).max() <= 2e-6
     assert np.all(got[pins, 48] == 1.0) and got[:, 48].sum() == len(pins)
@@ -158,7 +158,7 @@ def test_collect_matches_oracle_and_normalization():
         sur.collect(sim, ratio, 1)
         pos1, vel1 = cloth_state(mesh, sc.pins)
         f, t = sur.dataset(k * n, n)
-        ref = SO.features(pos, vel, sc.rows, sc.cols, h, T, wind)
+        ref = SO.features(pos, vel, sc.rows, sc.cols, h, T, wind, W.grid_positions(sc.rows, sc.cols, sc.cloth_args[2]))
         assert np.all(np.abs(f[:, :52] - ref[:, :52]) <= 1e-6 * np.maximum(1.0, np.abs(ref[:, :52])))
         s = T / h
         tref = (vel1[:, :3] - vel[:, :3]) * s
@@ -190,7 +190,9 @@ def test_coarse_step_matches_oracle():
     pos, vel = cloth_state(mesh, sc.pins)
     assert sim.step_surrogate(sur, ratio, 1) == 0
     pos1, vel1 = cloth_state(mesh, sc.pins)
-    rp, rv = SO.coarse_step(pos, vel, sc.rows, sc.cols, h, T, sc.config["wind"], p, in_mean, in_std, out_mean, out_std)
+    rest = W.grid_positions(sc.rows, sc.cols, sc.cloth_args[2])
+    rp, rv = SO.coarse_step(pos, vel, sc.rows, sc.cols, h, T, sc.config["wind"], rest, p, in_mean, in_std, out_mean,
+                            out_std)
     dv = np.abs(rv[:, :3] - vel[:, :3]).max()
     assert dv > 0
     assert np.abs(vel1[:, :3] - rv[:, :3]).max() <= 1e-2 * dv + 1e-7

@@ -64,22 +64,23 @@ def test_features_of_undeformed_cloth():
     for r in range(rows):
         for c in range(cols):
             pos[r * cols + c] = (c * h, r * h, 0.0, 0.01)
+    rest = pos[:, :3].copy()
     vel = np.zeros((rows * cols, 4), np.float32)
     vel[0, 3] = 1.0
     wind = (2.0, 0.0, 1.0)
-    f = SO.features(pos, vel, rows, cols, h, T, wind)
+    f = SO.features(pos, vel, rows, cols, h, T, wind, rest)
     interior = f[1 * cols + 2]
-    expect = np.array([(dc, dr, 0.0) for dr, dc in SO.NEIGHBOURS], np.float32).ravel()
-    assert np.allclose(interior[:24], expect, atol=1e-5)
-    assert np.all(interior[24:48] == 0)
+    assert np.all(f[:, :48] == 0)  # at rest: no deformation, no relative velocity
     s = np.float32(T) / np.float32(h)
     assert np.allclose(interior[49:52], np.array(wind, np.float32) * s)
     assert interior[52] == pytest.approx(0.5, abs=1e-6) and interior[53] == pytest.approx(0.5, abs=1e-6)
-    corner = f[0]
-    assert corner[48] == 1.0
-    assert np.all(corner[0:9] == 0) and np.all(corner[15:18] == 0)  # missing neighbours give zeros
-    assert np.allclose(corner[12:15], (1.0, 0.0, 0.0), atol=1e-5)  # (0, +1)
-    assert corner[52] == pytest.approx(0.5, abs=1e-6)
+    assert f[0, 48] == 1.0 and f[0, 52] == pytest.approx(0.5, abs=1e-6)
+    # stretch the right neighbour of the interior vertex by 0.02 in x
+    moved = pos.copy()
+    moved[1 * cols + 3, 0] += np.float32(0.02)
+    g = SO.features(moved, vel, rows, cols, h, T, wind, rest)[1 * cols + 2]
+    k = SO.NEIGHBOURS.index((0, 1))
+    assert g[3 * k] == pytest.approx(0.2, rel=1e-5) and np.all(np.delete(g[:24], 3 * k) == 0)
 
 
 def test_first_adam_step_closed_form():
