@@ -482,7 +482,7 @@ def main():
                     help="coarse steps between collected snapshots (0: c3 60; c4 coarse-steps/20, so that the "
                          "snapshots span the evaluated horizon)")
     ap.add_argument("--energy-growth", type=float, default=0.05)
-    ap.add_argument("--max-strain", type=float, default=100.0)
+    ap.add_argument("--max-strain", type=float, default=1000.0)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
