@@ -44,24 +44,25 @@ __device__ __forceinline__ float2 unpack_bf2(uint32_t u) {
 
 // GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its
 // slope 0.5 (1 + t) + 0.5 x (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 x^2), with
-// explicit fused multiply-adds (this file is compiled with -fmad=false).
+// the tanh argument as x (c + c a x^2) and explicit fused multiply-adds (this
+// file is compiled with -fmad=false).
+constexpr float kGeluCA = kGeluC * kGeluA;
+
 __device__ __forceinline__ float gelu(float x) {
-  const float x2 = x * x;
-  const float u = kGeluC * __fmaf_rn(kGeluA * x2, x, x);
+  const float u = __fmaf_rn(kGeluCA, x * x, kGeluC) * x;
   const float t = tc::tanh_fast(u);
-  const float hx = 0.5f * x;
-  return __fmaf_rn(hx, t, hx);
+  return x * __fmaf_rn(0.5f, t, 0.5f);
 }
 
 __device__ __forceinline__ void gelu_slope(float x, float& g, float& dg) {
   const float x2 = x * x;
-  const float u = kGeluC * __fmaf_rn(kGeluA * x2, x, x);
+  const float u = __fmaf_rn(kGeluCA, x2, kGeluC) * x;
   const float t = tc::tanh_fast(u);
-  const float hx = 0.5f * x;
-  g = __fmaf_rn(hx, t, hx);
+  const float half1pt = __fmaf_rn(0.5f, t, 0.5f);
+  g = x * half1pt;
   const float one_m_t2 = __fmaf_rn(-t, t, 1.0f);
-  const float du = kGeluC * __fmaf_rn(3.0f * kGeluA, x2, 1.0f);
-  dg = __fmaf_rn(hx * one_m_t2, du, __fmaf_rn(0.5f, t, 0.5f));
+  const float du = __fmaf_rn(3.0f * kGeluCA, x2, kGeluC);
+  dg = __fmaf_rn((0.5f * x) * one_m_t2, du, half1pt);
 }
 
 __device__ __forceinline__ void group_sync(int id) {
