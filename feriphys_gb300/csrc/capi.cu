@@ -1198,19 +1198,22 @@ int fgb_sim_get_timestep(const fgb_sim* s, double* seconds) {
 int fgb_sim_synchronize(fgb_sim* s, int* nonfinite) {
   if (!s) return fail(FGB_EINVAL, "null sim");
   int bad = 0;
+  unsigned all = 0;
   for (fgb_mesh* m : s->meshes) {
     if (m->stream) FGB_CUDA(cudaStreamSynchronize(m->stream));
     if (m->d_flags) {
       unsigned f = 0;
       FGB_CUDA(cudaMemcpy(&f, m->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
       if (f) {
-        bad = 1;
+        bad = bad || (f & 1u);
+        all |= f;
         FGB_CUDA(cudaMemsetAsync(m->d_flags, 0, sizeof(unsigned), m->stream));
         FGB_CUDA(cudaStreamSynchronize(m->stream));
       }
     }
   }
   if (nonfinite) *nonfinite = bad;
+  if (all & 2u) return fail(FGB_ECHECK, "a tile's staging copy did not complete in time");
   return FGB_OK;
 }
 

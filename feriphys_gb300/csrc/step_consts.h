@@ -49,7 +49,7 @@ struct StepConsts {
   float friction;
   int n_obstacle_faces;
   const void* obstacle_faces;  // ObsFace[n_obstacle_faces], flattened obstacle order
-  unsigned* flags;             // bit 0: a stepped vertex went non-finite
+  unsigned* flags;             // bit 0: a stepped vertex went non-finite; bit 1: a staging copy timed out
   ObsAccel accel;              // broad phase over obstacle_faces (enabled = 0: test all faces)
 };
 

@@ -6,10 +6,15 @@
 // order of the reference's scatter loops (strut ids ascending, then face ids
 // ascending -- checked on the host against the real ids before this kernel is
 // chosen), so the result is bit-identical to the general gather.
+#include <cuda.h>
+
+#include <cstring>
+
 #include "fastdiv.cuh"
 #include "grid_order.h"
 #include "kernels.h"
 #include "physics.cuh"
+#include "tc05.cuh"
 
 namespace fgb {
 
@@ -261,13 +266,14 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
                                           const float4* __restrict__ pos, const float4* __restrict__ vel,
                                           const float4* __restrict__ force_in, float4* __restrict__ pos_out,
                                           float4* __restrict__ vel_out, const StepConsts& c, V3<float> wind,
-                                          unsigned* flags) {
+                                          unsigned* flags, const CUtensorMap* map_pos = nullptr,
+                                          const CUtensorMap* map_vel = nullptr) {
   using G = TileGeom<TW, TH>;
   using I = Interior<TW, TH>;
   constexpr int NMAIN = TW * TH, NT = TW * TH + HALO;
   static_assert(HALO == 2 * TW && TW + 2 * TH + 1 <= 2 * TW && TW >= 32, "helper layout assumes 64 helpers");
   constexpr int EW = G::EW, OW = I::OW, NO = I::NO, QW = I::QW, NQ = I::NQ;
-  extern __shared__ float4 s_dyn[];
+  extern __shared__ __align__(128) float4 s_dyn[];
   float4* s_pos = s_dyn;
   float4* s_vel = s_dyn + G::EH * G::EW;
   float4* s_su = s_dyn + 2 * G::EH * G::EW;                  // [5][NO] unit vector, s1
@@ -293,12 +299,27 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   const bool vertex = tid < NMAIN && (INTERIOR || (r < R && cc < C));
   V3<float> F{c.force0[0], c.force0[1], c.force0[2]};
 
-  // ---- stage positions/velocities; prefetch the strut constants this thread needs
-  for (int i = tid; i < G::EH * G::EW; i += NT) {
-    const int gr = r0 - 2 + i / G::EW, gc = c0 - 2 + i % G::EW;
-    if (INTERIOR || (gr >= 0 && gr < R && gc >= 0 && gc < C)) {
-      s_pos[i] = pos[gr * C + gc];
-      s_vel[i] = vel[gr * C + gc];
+  // ---- stage positions/velocities; prefetch the strut constants this thread needs.
+  // With tensor maps, one thread asks the TMA engine for the two (TH+4) x (TW+4)
+  // boxes (rows r0-2.., columns c0-2..; outside the cloth they read zeros, which
+  // no thread uses) while every thread loads its strut constants.
+  __shared__ uint64_t tma_bar;
+  const bool tma = map_pos != nullptr && (tc::smem_u32(s_pos) & 127u) == 0;
+  if (tma) {
+    if (tid == 0) {
+      tc::mbar_init(&tma_bar, 1);
+      tc::mbar_fence_init();
+      tc::mbar_arrive_expect_tx(&tma_bar, 2u * G::EH * G::EW * 16u);
+      tc::tma_load_2d(s_pos, map_pos, 4 * (c0 - 2), r0 - 2, &tma_bar);
+      tc::tma_load_2d(s_vel, map_vel, 4 * (c0 - 2), r0 - 2, &tma_bar);
+    }
+  } else {
+    for (int i = tid; i < G::EH * G::EW; i += NT) {
+      const int gr = r0 - 2 + i / G::EW, gc = c0 - 2 + i % G::EW;
+      if (INTERIOR || (gr >= 0 && gr < R && gc >= 0 && gc < C)) {
+        s_pos[i] = pos[gr * C + gc];
+        s_vel[i] = vel[gr * C + gc];
+      }
     }
   }
   const int h = tid - NMAIN;
@@ -361,6 +382,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   }
   if (!INTERIOR && quad_r > -3 && !quad_exists(r0 + quad_r, c0 + quad_c, R, C)) quad_r = -3;
   __syncthreads();
+  if (tma && !tc::mbar_wait(&tma_bar, 0) && flags) atomicOr(flags, 2u);  // bounded: a stuck copy is reported
 
   // ---- compute every strut and face of the tile once
   auto put = [&](int kind, int rr, int ccl, float k, float cd, float L) {
@@ -457,17 +479,22 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
                                                                       const float4* __restrict__ vel,
                                                                       const float4* __restrict__ force_in,
                                                                       float4* __restrict__ pos_out,
-                                                                      float4* __restrict__ vel_out, StepConsts c) {
+                                                                      float4* __restrict__ vel_out, StepConsts c,
+                                                                      const __grid_constant__ CUtensorMap map_pos,
+                                                                      const __grid_constant__ CUtensorMap map_vel,
+                                                                      int use_tma) {
   const int b = blockIdx.x;
+  const CUtensorMap* mp = use_tma ? &map_pos : nullptr;
+  const CUtensorMap* mv = use_tma ? &map_vel : nullptr;
   if (b < n_ring) {
     int bx, by;
     ring_tile(split, b, bx, by);
     tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
-                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags);
+                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv);
   } else {
     const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
     tile_step<TW, TH, HALO, true>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel, force_in,
-                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags);
+                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv);
   }
 }
 
@@ -513,6 +540,34 @@ size_t tiled_smem_bytes() {
   using G = TileGeom<kTileW, kTileH>;
   using I = Interior<kTileW, kTileH>;
   return 2 * sizeof(float4) * G::EH * G::EW + size_t(I::BYTES);
+}
+
+// Tensor map of one float4 state array of an R x C grid, seen as R rows of
+// 4C floats, with the tiled kernel's staging box ((TW+4) float4 x (TH+4) rows).
+bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<Encode>(fn);
+    else
+      cudaGetLastError();
+  }
+  if (!encode || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+  const cuuint64_t dims[2] = {4ull * cuuint64_t(C), cuuint64_t(R)};
+  const cuuint64_t strides[1] = {16ull * cuuint64_t(C)};
+  const cuuint32_t box[2] = {4u * (kTileW + 4), kTileH + 4};
+  const cuuint32_t elem[2] = {1, 1};
+  return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4*>(base), dims, strides, box, elem,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
@@ -600,8 +655,13 @@ cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4*
       if (e != cudaSuccess) return e;
       attr_set = true;
     }
+    CUtensorMap map_pos, map_vel;
+    std::memset(&map_pos, 0, sizeof(map_pos));
+    std::memset(&map_vel, 0, sizeof(map_vel));
+    const int use_tma =
+        encode_state_map(&map_pos, pos, g.rows, g.cols) && encode_state_map(&map_vel, vel, g.rows, g.cols) ? 1 : 0;
     k_step_grid_tiled<kTileW, kTileH, kHalo><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
-        g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c);
+        g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c, map_pos, map_vel, use_tma);
   }
   return cudaGetLastError();
 }

@@ -17,6 +17,7 @@
 // (Both orientations were checked against a host GEMM on the GPU.)
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -167,6 +168,18 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+
+// Tiled TMA load of a 2D box (the tensor map's box size) at element
+// coordinates (x, y) into shared memory (128-byte aligned); completion counts
+// the box's bytes on the mbarrier.  x times the element size must be a
+// multiple of 16 bytes; negative or out-of-range coordinates read zeros.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(mbar))
       : "memory");
 }
 
