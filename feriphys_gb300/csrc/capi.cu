@@ -419,6 +419,23 @@ int prepare_batch(fgb_sim* s) {
     }
     FGB_CUDA(cudaMemcpyAsync(s->d_desc, desc.data(), desc.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice,
                              bs));
+    // TMA staging maps for every cloth's buffers (all or none)
+    std::vector<unsigned char> maps(desc.size() * fgb::kClothMapBytes + 64);
+    unsigned char* mp = maps.data() + ((64 - (reinterpret_cast<uintptr_t>(maps.data()) & 63)) & 63);
+    bool maps_ok = true;
+    for (size_t i = 0; i < desc.size() && maps_ok; ++i) maps_ok = fgb::encode_cloth_maps(desc[i], mp + i * fgb::kClothMapBytes);
+    if (maps_ok) {
+      if (s->d_maps_cap < desc.size()) {
+        FGB_CUDA(dalloc(s->d_maps, desc.size() * fgb::kClothMapBytes));
+        s->d_maps_cap = desc.size();
+        drop_graphs(s);
+      }
+      FGB_CUDA(cudaMemcpyAsync(s->d_maps, mp, desc.size() * fgb::kClothMapBytes, cudaMemcpyHostToDevice, bs));
+    } else {
+      dfree(s->d_maps);
+      s->d_maps_cap = 0;
+      drop_graphs(s);
+    }
     FGB_CUDA(cudaStreamSynchronize(bs));
     s->desc = std::move(desc);
   }
@@ -430,7 +447,7 @@ int batch_launch(fgb_sim* s, int parity, int mode, int ctas) {
   cudaStream_t st = batch_stream(s);
   FGB_CUDA(cudaMemsetAsync(s->d_counter, 0, sizeof(int), st));
   FGB_CUDA(fgb::launch_step_batched(s->d_desc, s->d_work, s->n_work, s->d_counter, parity, mode, ctas,
-                                    make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st));
+                                    make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st, s->d_maps));
   return FGB_OK;
 }
 
@@ -1227,6 +1244,7 @@ int fgb_sim_destroy(fgb_sim* s) {
   dfree(s->d_desc);
   dfree(s->d_work);
   dfree(s->d_counter);
+  dfree(s->d_maps);
   delete s;
   return FGB_OK;
 }

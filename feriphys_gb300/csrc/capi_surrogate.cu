@@ -405,7 +405,7 @@ int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing,
   for (uint32_t j = 0; j < ratio && n_fw > 0; ++j) {
     FGB_CUDA(cudaMemsetAsync(g->d_fcounter, 0, sizeof(int), st));
     FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, g->d_fwork, n_fw, g->d_fcounter, from ^ int(j & 1u), 1, ctas, fc,
-                                      st));
+                                      st, s->d_maps));
   }
   FGB_CUDA(cudaStreamSynchronize(st));  // the host table must outlive its upload
   return FGB_OK;

@@ -104,6 +104,8 @@ struct fgb_sim {
   int4* d_work = nullptr;
   int n_work = 0;
   std::vector<int> work_host;             // host copy of the work list (4 ints per item)
+  unsigned char* d_maps = nullptr;        // per batch cloth: 4 tensor maps for TMA staging (null: thread staging)
+  size_t d_maps_cap = 0;
   int* d_counter = nullptr;
   int parity = 0;
   int mode = -1, ctas = 0;                // launch form chosen by the tuner

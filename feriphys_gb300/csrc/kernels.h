@@ -63,8 +63,15 @@ void batch_tiles(int cloth, int rows, int cols, int* out4 /* may be null */, int
 
 // mode 0: one CTA per work item; mode 1: persistent CTAs pulling items from
 // *counter (reset to 0 by the caller before the launch).
+// maps: null, or per cloth 4 tensor maps {pos[0], vel[0], pos[1], vel[1]}
+// (encode_cloth_maps) for TMA staging of the tiles.
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
-                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s);
+                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s,
+                                const void* maps = nullptr);
+// Size of one cloth's tensor maps (4 x 128 bytes) and their encoding; false
+// when the driver's encoder is unavailable or an address is misaligned.
+constexpr size_t kClothMapBytes = 4 * 128;
+bool encode_cloth_maps(const ClothDesc& d, void* out /* kClothMapBytes, 64-byte aligned */);
 int batched_ctas_per_sm();
 
 }  // namespace fgb

@@ -267,7 +267,8 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
                                           const float4* __restrict__ force_in, float4* __restrict__ pos_out,
                                           float4* __restrict__ vel_out, const StepConsts& c, V3<float> wind,
                                           unsigned* flags, const CUtensorMap* map_pos = nullptr,
-                                          const CUtensorMap* map_vel = nullptr) {
+                                          const CUtensorMap* map_vel = nullptr, uint64_t* tma_bar = nullptr,
+                                          uint32_t tma_phase = 0) {
   using G = TileGeom<TW, TH>;
   using I = Interior<TW, TH>;
   constexpr int NMAIN = TW * TH, NT = TW * TH + HALO;
@@ -303,15 +304,14 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   // With tensor maps, one thread asks the TMA engine for the two (TH+4) x (TW+4)
   // boxes (rows r0-2.., columns c0-2..; outside the cloth they read zeros, which
   // no thread uses) while every thread loads its strut constants.
-  __shared__ uint64_t tma_bar;
-  const bool tma = map_pos != nullptr && (tc::smem_u32(s_pos) & 127u) == 0;
+  // (tma_bar: an mbarrier the kernel initialised once; tma_phase: the parity
+  // of its phase this tile completes)
+  const bool tma = map_pos != nullptr && tma_bar != nullptr && (tc::smem_u32(s_pos) & 127u) == 0;
   if (tma) {
     if (tid == 0) {
-      tc::mbar_init(&tma_bar, 1);
-      tc::mbar_fence_init();
-      tc::mbar_arrive_expect_tx(&tma_bar, 2u * G::EH * G::EW * 16u);
-      tc::tma_load_2d(s_pos, map_pos, 4 * (c0 - 2), r0 - 2, &tma_bar);
-      tc::tma_load_2d(s_vel, map_vel, 4 * (c0 - 2), r0 - 2, &tma_bar);
+      tc::mbar_arrive_expect_tx(tma_bar, 2u * G::EH * G::EW * 16u);
+      tc::tma_load_2d(s_pos, map_pos, 4 * (c0 - 2), r0 - 2, tma_bar);
+      tc::tma_load_2d(s_vel, map_vel, 4 * (c0 - 2), r0 - 2, tma_bar);
     }
   } else {
     for (int i = tid; i < G::EH * G::EW; i += NT) {
@@ -382,7 +382,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   }
   if (!INTERIOR && quad_r > -3 && !quad_exists(r0 + quad_r, c0 + quad_c, R, C)) quad_r = -3;
   __syncthreads();
-  if (tma && !tc::mbar_wait(&tma_bar, 0) && flags) atomicOr(flags, 2u);  // bounded: a stuck copy is reported
+  if (tma && !tc::mbar_wait(tma_bar, tma_phase) && flags) atomicOr(flags, 2u);  // bounded: a stuck copy is reported
 
   // ---- compute every strut and face of the tile once
   auto put = [&](int kind, int rr, int ccl, float k, float cd, float L) {
@@ -483,18 +483,24 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
                                                                       const __grid_constant__ CUtensorMap map_pos,
                                                                       const __grid_constant__ CUtensorMap map_vel,
                                                                       int use_tma) {
+  __shared__ uint64_t bar;
   const int b = blockIdx.x;
   const CUtensorMap* mp = use_tma ? &map_pos : nullptr;
   const CUtensorMap* mv = use_tma ? &map_vel : nullptr;
+  if (use_tma && threadIdx.x == 0) {  // the same thread issues the copies after this
+    tc::mbar_init(&bar, 1);
+    tc::mbar_fence_init();
+  }
   if (b < n_ring) {
     int bx, by;
     ring_tile(split, b, bx, by);
     tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
-                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv);
+                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv, &bar, 0);
   } else {
     const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
     tile_step<TW, TH, HALO, true>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel, force_in,
-                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv);
+                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv,
+                                  &bar, 0);
   }
 }
 
@@ -506,8 +512,15 @@ template <int TW, int TH, int HALO>
 __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothDesc* __restrict__ cloths,
                                                                    const int4* __restrict__ work, int n_work,
                                                                    int* __restrict__ counter, int parity,
-                                                                   int persistent, StepConsts c) {
+                                                                   int persistent, StepConsts c,
+                                                                   const CUtensorMap* __restrict__ maps) {
   __shared__ int s_item;
+  __shared__ uint64_t bar;
+  uint32_t phase = 0;
+  if (maps && threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::mbar_fence_init();
+  }
   int item = blockIdx.x;
   while (true) {
     if (persistent) {
@@ -524,12 +537,18 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothD
       continue;
     }
     const V3<float> wind{d.wind[0], d.wind[1], d.wind[2]};
+    // maps: per cloth, {pos[0], vel[0], pos[1], vel[1]} (empty maps: thread staging)
+    const CUtensorMap* mp = maps ? maps + 4 * size_t(w.x) + 2 * parity : nullptr;
+    const CUtensorMap* mv = mp ? mp + 1 : nullptr;
     if (w.w)
       tile_step<TW, TH, HALO, true>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
-                                    d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags);
+                                    d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
+                                    maps ? &bar : nullptr, phase);
     else
       tile_step<TW, TH, HALO, false>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
-                                     d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags);
+                                     d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
+                                     maps ? &bar : nullptr, phase);
+    phase ^= maps ? 1u : 0u;
     if (!persistent) break;
   }
 }
@@ -572,6 +591,14 @@ bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C) {
 
 }  // namespace
 
+bool encode_cloth_maps(const ClothDesc& d, void* out) {
+  CUtensorMap* m = static_cast<CUtensorMap*>(out);
+  for (int k = 0; k < 2; ++k)
+    if (!encode_state_map(m + 2 * k, d.pos[k], d.rows, d.cols) || !encode_state_map(m + 2 * k + 1, d.vel[k], d.rows, d.cols))
+      return false;
+  return true;
+}
+
 void batch_tiles(int cloth, int rows, int cols, int* out4, int* n_ring, int* n_interior) {
   TileSplit t;
   t.tx = (cols + kTileW - 1) / kTileW;
@@ -612,7 +639,7 @@ int batched_ctas_per_sm() {
 }
 
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
-                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s) {
+                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s, const void* maps) {
   if (n_work <= 0) return cudaSuccess;
   const size_t smem = tiled_smem_bytes();
   static bool attr_set = false;
@@ -623,8 +650,8 @@ cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n
     attr_set = true;
   }
   const int grid = mode == 1 ? (persistent_ctas < n_work ? persistent_ctas : n_work) : n_work;
-  k_step_batched<kTileW, kTileH, kHalo><<<grid, kTileW * kTileH + kHalo, smem, s>>>(cloths, work, n_work, counter,
-                                                                                    parity, mode == 1, c);
+  k_step_batched<kTileW, kTileH, kHalo><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
+      cloths, work, n_work, counter, parity, mode == 1, c, static_cast<const CUtensorMap*>(maps));
   return cudaGetLastError();
 }
 
