@@ -99,6 +99,20 @@ struct fgb_surrogate {
   size_t fwork_cap = 0;
   int* d_fcounter = nullptr;
   int groups = 4;
+  // checked rollout decided on the device (per cloth: accepted energy, margin
+  // scale, verdict; per batch cloth: work-list range, mesh index, compacted
+  // position; counters: this step's failures, fallback items, running total)
+  float* d_e_old = nullptr;
+  size_t e_old_cap = 0;
+  double* d_e_ref = nullptr;
+  size_t e_ref_cap = 0;
+  int* d_fail = nullptr;
+  size_t fail_cap = 0;
+  int* d_bidx = nullptr;  // 4 x n_batch: off, cnt, mesh, dst
+  size_t bidx_cap = 0;
+  int* d_counts = nullptr;  // [0] failures this step, [1] fallback items
+  unsigned long long* d_total = nullptr;
+  cudaStream_t side = nullptr;  // captures the fallback body
 };
 
 namespace {
@@ -411,6 +425,229 @@ int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing,
   return FGB_OK;
 }
 
+// ---- checked rollout decided on the device ---------------------------------
+
+constexpr int kHostDecides = 1;  // not an error: run the host-decided loop instead
+
+// Inputs of the graph-built rollout that stay fixed for one call.
+struct Rollout {
+  uint32_t ratio = 1;
+  int n_tiles = 0, n_cloths = 0, n_batch = 0, ctas = 1;
+  fgb::StepConsts coarse, fine;
+  float3 gforce;
+  float growth = 0.0f, abs_margin = 0.0f, max_strain = 0.0f;
+};
+
+// The fallback of the cloths that failed this step (the body of the graph's
+// conditional): the same fine steps as fine_fallback, with the failing set
+// and the compacted work list made on the device, then a re-check whose
+// energies the failing cloths accept.  Launched on `bs` while it captures.
+int capture_fallback(fgb_surrogate* g, fgb_sim* s, const Rollout& ro, int par, cudaStream_t bs) {
+  if (s->batch.empty()) {
+    fgb_mesh* m = s->meshes[0];
+    const fgb::GridTopo gt{int(m->topo.rows), int(m->topo.cols), m->d_grid, 0};
+    fgb::StepConsts mc = ro.fine;
+    mc.flags = m->d_flags;
+    int a = par;
+    for (uint32_t j = 0; j < ro.ratio; ++j, a ^= 1)
+      FGB_CUDA(fgb::launch_step_grid(gt, static_cast<const float4*>(m->pos[a]), static_cast<const float4*>(m->vel[a]),
+                                     nullptr, static_cast<float4*>(m->pos[a ^ 1]), static_cast<float4*>(m->vel[a ^ 1]),
+                                     mc, bs));
+    if (a != (par ^ 1)) {
+      const size_t bytes = size_t(m->topo.n) * sizeof(float4);
+      FGB_CUDA(cudaMemcpyAsync(m->pos[par ^ 1], m->pos[a], bytes, cudaMemcpyDeviceToDevice, bs));
+      FGB_CUDA(cudaMemcpyAsync(m->vel[par ^ 1], m->vel[a], bytes, cudaMemcpyDeviceToDevice, bs));
+    }
+  } else {
+    const int nb = ro.n_batch;
+    int* off = g->d_bidx;
+    int* cnt = off + nb;
+    int* mesh = cnt + nb;
+    int* dst = mesh + nb;
+    FGB_CUDA(S::launch_fallback_tables(s->d_desc, mesh, nb, g->d_fail, off, cnt, s->d_work, g->d_fdesc, dst,
+                                       g->d_fwork, g->d_counts + 1, bs));
+    int from = par;
+    if ((ro.ratio & 1u) == 0) {
+      FGB_CUDA(S::launch_copy_unskipped(g->d_fdesc, nb, par, bs));
+      from = par ^ 1;
+    }
+    for (uint32_t j = 0; j < ro.ratio; ++j) {
+      FGB_CUDA(cudaMemsetAsync(g->d_fcounter, 0, sizeof(int), bs));
+      FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, g->d_fwork, s->n_work, g->d_fcounter, from ^ int(j & 1u), 1,
+                                        ro.ctas, ro.fine, bs, s->d_maps, g->d_counts + 1));
+    }
+  }
+  FGB_CUDA(S::launch_check(g->d_cloths, g->d_tiles, ro.n_tiles, ro.n_cloths, par ^ 1, ro.gforce, g->d_tile_chk,
+                           g->d_cloth_chk, bs));
+  FGB_CUDA(S::launch_accept(g->d_cloth_chk, ro.n_cloths, g->d_fail, g->d_e_old, bs));
+  return FGB_OK;
+}
+
+// One coarse step from buffers [par] as a graph: surrogate step, check,
+// verdicts, and the fallback body under an IF conditional the verdict
+// kernel sets.
+int capture_checked_step(fgb_surrogate* g, fgb_sim* s, const Rollout& ro, int par, cudaStream_t st,
+                         cudaGraphExec_t* out) {
+  FGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = FGB_OK;
+  cudaError_t e = cudaSuccess;
+  do {
+    if ((e = cudaMemsetAsync(g->d_counts, 0, sizeof(int), st)) != cudaSuccess) break;
+    if ((e = S::launch_sur_step(g->d_cloths, g->d_tiles, ro.n_tiles, par, g->d_blob, g->norm, ro.coarse, g->groups, 0,
+                                g->d_err, st)) != cudaSuccess)
+      break;
+    if ((e = S::launch_check(g->d_cloths, g->d_tiles, ro.n_tiles, ro.n_cloths, par ^ 1, ro.gforce, g->d_tile_chk,
+                             g->d_cloth_chk, st)) != cudaSuccess)
+      break;
+    if ((e = S::launch_decide(g->d_cloth_chk, ro.n_cloths, g->d_e_old, g->d_e_ref, ro.growth, ro.abs_margin,
+                              ro.max_strain, g->d_fail, g->d_counts, st)) != cudaSuccess)
+      break;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr)) != cudaSuccess) break;
+    cudaGraphConditionalHandle h;
+    if ((e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    if ((e = S::launch_set_fallback(h, g->d_counts, g->d_total, st)) != cudaSuccess) break;
+    if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) break;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // the other members zero
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    if ((e = cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &cp)) != cudaSuccess) break;
+    if ((e = cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+        cudaSuccess)
+      break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(g->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+      break;
+    rc = capture_fallback(g, s, ro, par, g->side);
+    cudaGraph_t body_out = nullptr;
+    const cudaError_t eb = cudaStreamEndCapture(g->side, &body_out);
+    if (rc == FGB_OK && eb != cudaSuccess) e = eb;
+  } while (false);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+  if (rc == FGB_OK && e == cudaSuccess) e = ee;
+  if (rc != FGB_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc != FGB_OK ? rc : fail(FGB_ECUDA, cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  FGB_CUDA(e);
+  return FGB_OK;
+}
+
+// The checked rollout with every decision on the device: one graph launch
+// per coarse step and one host wait at the end.  Decisions, fallbacks and
+// states equal the host-decided loop's (the same kernels; the verdict is the
+// same double-precision test).  Returns kHostDecides before touching the
+// state when the graph cannot be built (the caller then decides on the host).
+int rollout_on_device(fgb_surrogate* g, fgb_sim* s, uint32_t ratio, uint64_t n_coarse,
+                      const fgb_surrogate_check* chk, int n_tiles, const fgb::StepConsts& cst,
+                      const std::vector<float2>& e_old, const std::vector<double>& e_ref, cudaStream_t st,
+                      uint64_t* n_fallbacks) {
+  Rollout ro;
+  ro.ratio = ratio;
+  ro.n_tiles = n_tiles;
+  ro.n_cloths = int(s->meshes.size());
+  ro.n_batch = int(s->batch.size());
+  ro.coarse = cst;
+  ro.fine = fgb::detail::make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel);
+  ro.gforce = make_float3(s->cfg.gravity[0], s->cfg.gravity[1], s->cfg.gravity[2]);
+  ro.growth = chk->energy_growth;
+  ro.abs_margin = chk->energy_abs;
+  ro.max_strain = chk->max_strain;
+  const int nc = ro.n_cloths, nb = ro.n_batch;
+  if (nb == 0 && nc != 1) return kHostDecides;
+  std::vector<int> bidx;
+  if (nb > 0) {
+    // each batch cloth's work items are one contiguous range of the list
+    bidx.assign(4 * size_t(nb), 0);
+    std::vector<char> seen(nb, 0);
+    int prev = -1;
+    for (size_t i = 0; i + 3 < s->work_host.size(); i += 4) {
+      const int b = s->work_host[i];
+      if (b < 0 || b >= nb) return kHostDecides;
+      if (b != prev) {
+        if (seen[b]) return kHostDecides;
+        seen[b] = 1;
+        bidx[b] = int(i / 4);
+        prev = b;
+      }
+      ++bidx[nb + b];
+    }
+    for (int b = 0; b < nb; ++b) {
+      const size_t mi = size_t(std::find(s->meshes.begin(), s->meshes.end(), s->batch[b]) - s->meshes.begin());
+      if (mi >= s->meshes.size()) return kHostDecides;
+      bidx[2 * nb + b] = int(mi);
+    }
+    int ctas = s->ctas;
+    if (s->mode != 1 || ctas <= 0) {
+      int dev = 0, sms = 1;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      ctas = fgb::batched_ctas_per_sm() * sms;
+    }
+    ro.ctas = std::max(1, std::min(ctas, s->n_work));
+    FGB_CUDA(dgrow(g->d_bidx, g->bidx_cap, bidx.size(), sizeof(int)));
+    FGB_CUDA(dgrow(g->d_fdesc, g->fdesc_cap, size_t(nb), sizeof(fgb::ClothDesc)));
+    FGB_CUDA(dgrow(g->d_fwork, g->fwork_cap, size_t(std::max(s->n_work, 1)), sizeof(int4)));
+    if (!g->d_fcounter) FGB_CUDA(cudaMalloc(&g->d_fcounter, sizeof(int)));
+  }
+  FGB_CUDA(dgrow(g->d_e_old, g->e_old_cap, size_t(nc), sizeof(float)));
+  FGB_CUDA(dgrow(g->d_e_ref, g->e_ref_cap, size_t(nc), sizeof(double)));
+  FGB_CUDA(dgrow(g->d_fail, g->fail_cap, size_t(nc), sizeof(int)));
+  if (!g->d_counts) FGB_CUDA(cudaMalloc(&g->d_counts, 2 * sizeof(int)));
+  if (!g->d_total) FGB_CUDA(cudaMalloc(&g->d_total, sizeof(unsigned long long)));
+  if (!g->side) FGB_CUDA(cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking));
+  std::vector<float> e0(nc);
+  for (int c = 0; c < nc; ++c) e0[c] = e_old[c].x;
+  FGB_CUDA(cudaMemcpyAsync(g->d_e_old, e0.data(), nc * sizeof(float), cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(g->d_e_ref, e_ref.data(), nc * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (nb > 0)
+    FGB_CUDA(cudaMemcpyAsync(g->d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemsetAsync(g->d_total, 0, sizeof(unsigned long long), st));
+  FGB_CUDA(cudaStreamSynchronize(st));  // the host tables must outlive their upload
+  FGB_CUDA(S::prime_sur_step(g->groups));
+  FGB_CUDA(fgb::prime_step_kernels());
+
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  const int p0 = s->parity;
+  int rc = capture_checked_step(g, s, ro, p0, st, &exec[p0]);
+  if (rc == FGB_OK && n_coarse > 1) rc = capture_checked_step(g, s, ro, p0 ^ 1, st, &exec[p0 ^ 1]);
+  if (rc != FGB_OK) {
+    for (cudaGraphExec_t x : exec)
+      if (x) cudaGraphExecDestroy(x);
+    cudaGetLastError();
+    return kHostDecides;
+  }
+  cudaError_t e = cudaSuccess;
+  for (uint64_t k = 0; k < n_coarse && e == cudaSuccess; ++k) {
+    e = cudaGraphLaunch(exec[s->parity], st);
+    if (e != cudaSuccess) break;
+    s->parity ^= 1;
+    for (fgb_mesh* m : s->meshes) {
+      m->cur = s->parity;
+      m->has_force = false;
+      m->staged = false;
+    }
+  }
+  unsigned long long total = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, g->d_total, sizeof(total), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  for (cudaGraphExec_t x : exec)
+    if (x) cudaGraphExecDestroy(x);
+  FGB_CUDA(e);
+  if (n_fallbacks) *n_fallbacks = total;
+  return FGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -491,6 +728,13 @@ int fgb_surrogate_destroy(fgb_surrogate* g) {
   dfree(g->d_fdesc);
   dfree(g->d_fwork);
   dfree(g->d_fcounter);
+  dfree(g->d_e_old);
+  dfree(g->d_e_ref);
+  dfree(g->d_fail);
+  dfree(g->d_bidx);
+  dfree(g->d_counts);
+  dfree(g->d_total);
+  if (g->side) cudaStreamDestroy(g->side);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
   return FGB_OK;
@@ -760,6 +1004,10 @@ int fgb_sim_step_surrogate(fgb_sim* s, fgb_surrogate* g, uint32_t ratio, uint64_
     // the margin's scale is fixed for the whole call, so the allowed growth is
     // linear in the number of coarse steps, never compounding
     for (size_t c = 0; c < s->meshes.size(); ++c) e_ref[c] += std::fabs(double(e_old[c].x));
+  }
+  if (checks && s->graphs) {
+    const int rd = rollout_on_device(g, s, ratio, n_coarse, chk, n_tiles, cst, e_old, e_ref, st, n_fallbacks);
+    if (rd != kHostDecides) return rd == FGB_OK ? check_err(g, st) : rd;
   }
   uint64_t fallbacks = 0;
   std::vector<int> failing;

@@ -64,10 +64,15 @@ void batch_tiles(int cloth, int rows, int cols, int* out4 /* may be null */, int
 // mode 0: one CTA per work item; mode 1: persistent CTAs pulling items from
 // *counter (reset to 0 by the caller before the launch).
 // maps: null, or per cloth 4 tensor maps {pos[0], vel[0], pos[1], vel[1]}
-// (encode_cloth_maps) for TMA staging of the tiles.
+// (encode_cloth_maps) for TMA staging of the tiles.  n_work_dev: null, or the
+// item count in device memory (mode 1 only; n_work is then its upper bound,
+// which sizes the grid).
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
                                 int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s,
-                                const void* maps = nullptr);
+                                const void* maps = nullptr, const int* n_work_dev = nullptr);
+// Sets the launch attributes of the tiled and batched step kernels (done by
+// their launchers on first use; call it before a stream capture).
+cudaError_t prime_step_kernels();
 // Size of one cloth's tensor maps (4 x 128 bytes) and their encoding; false
 // when the driver's encoder is unavailable or an address is misaligned.
 constexpr size_t kClothMapBytes = 4 * 128;

@@ -261,7 +261,7 @@ __device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, in
 
 // One tile of one cloth.  No early return: the batched kernel runs it in a
 // loop, so every thread reaches the end of every tile.
-template <int TW, int TH, int HALO, bool INTERIOR>
+template <int TW, int TH, int HALO, bool INTERIOR, bool TMA = false>
 __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const float4* __restrict__ planes,
                                           const float4* __restrict__ pos, const float4* __restrict__ vel,
                                           const float4* __restrict__ force_in, float4* __restrict__ pos_out,
@@ -306,7 +306,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   // no thread uses) while every thread loads its strut constants.
   // (tma_bar: an mbarrier the kernel initialised once; tma_phase: the parity
   // of its phase this tile completes)
-  const bool tma = map_pos != nullptr && tma_bar != nullptr && (tc::smem_u32(s_pos) & 127u) == 0;
+  const bool tma = TMA && (tc::smem_u32(s_pos) & 127u) == 0;
   if (tma) {
     if (tid == 0) {
       tc::mbar_arrive_expect_tx(tma_bar, 2u * G::EH * G::EW * 16u);
@@ -472,7 +472,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
 
 // One launch for all tiles: the boundary ring first (its tiles are slower
 // and then overlap the interior ones instead of running as a lone wave).
-template <int TW, int TH, int HALO>
+template <int TW, int TH, int HALO, bool TMA>
 __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, int C, TileSplit split, int n_ring,
                                                                       const float4* __restrict__ planes,
                                                                       const float4* __restrict__ pos,
@@ -481,26 +481,25 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
                                                                       float4* __restrict__ pos_out,
                                                                       float4* __restrict__ vel_out, StepConsts c,
                                                                       const __grid_constant__ CUtensorMap map_pos,
-                                                                      const __grid_constant__ CUtensorMap map_vel,
-                                                                      int use_tma) {
+                                                                      const __grid_constant__ CUtensorMap map_vel) {
   __shared__ uint64_t bar;
   const int b = blockIdx.x;
-  const CUtensorMap* mp = use_tma ? &map_pos : nullptr;
-  const CUtensorMap* mv = use_tma ? &map_vel : nullptr;
-  if (use_tma && threadIdx.x == 0) {  // the same thread issues the copies after this
+  const CUtensorMap* mp = &map_pos;
+  const CUtensorMap* mv = &map_vel;
+  if (TMA && threadIdx.x == 0) {  // the same thread issues the copies after this
     tc::mbar_init(&bar, 1);
     tc::mbar_fence_init();
   }
   if (b < n_ring) {
     int bx, by;
     ring_tile(split, b, bx, by);
-    tile_step<TW, TH, HALO, false>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
-                                   V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv, &bar, 0);
+    tile_step<TW, TH, HALO, false, TMA>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
+                                        V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv, &bar, 0);
   } else {
     const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
-    tile_step<TW, TH, HALO, true>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel, force_in,
-                                  pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv,
-                                  &bar, 0);
+    tile_step<TW, TH, HALO, true, TMA>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel,
+                                       force_in, pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]},
+                                       c.flags, mp, mv, &bar, 0);
   }
 }
 
@@ -508,16 +507,18 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
 // come from a list packed on the host (largest cloths first, each cloth's
 // boundary tiles before its interior ones); in persistent mode every CTA
 // pulls items from a global counter until the list is exhausted.
-template <int TW, int TH, int HALO>
+template <int TW, int TH, int HALO, bool TMA>
 __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothDesc* __restrict__ cloths,
                                                                    const int4* __restrict__ work, int n_work,
                                                                    int* __restrict__ counter, int parity,
                                                                    int persistent, StepConsts c,
-                                                                   const CUtensorMap* __restrict__ maps) {
+                                                                   const CUtensorMap* __restrict__ maps,
+                                                                   const int* __restrict__ n_work_dev) {
   __shared__ int s_item;
+  if (n_work_dev) n_work = *n_work_dev;  // a count made on the device (persistent mode)
   __shared__ uint64_t bar;
   uint32_t phase = 0;
-  if (maps && threadIdx.x == 0) {
+  if (TMA && threadIdx.x == 0) {
     tc::mbar_init(&bar, 1);
     tc::mbar_fence_init();
   }
@@ -538,17 +539,17 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothD
     }
     const V3<float> wind{d.wind[0], d.wind[1], d.wind[2]};
     // maps: per cloth, {pos[0], vel[0], pos[1], vel[1]} (empty maps: thread staging)
-    const CUtensorMap* mp = maps ? maps + 4 * size_t(w.x) + 2 * parity : nullptr;
-    const CUtensorMap* mv = mp ? mp + 1 : nullptr;
+    const CUtensorMap* mp = TMA ? maps + 4 * size_t(w.x) + 2 * parity : nullptr;
+    const CUtensorMap* mv = TMA ? mp + 1 : nullptr;
     if (w.w)
-      tile_step<TW, TH, HALO, true>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
-                                    d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
-                                    maps ? &bar : nullptr, phase);
+      tile_step<TW, TH, HALO, true, TMA>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity],
+                                         d.force_in, d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
+                                         &bar, phase);
     else
-      tile_step<TW, TH, HALO, false>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity], d.force_in,
-                                     d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
-                                     maps ? &bar : nullptr, phase);
-    phase ^= maps ? 1u : 0u;
+      tile_step<TW, TH, HALO, false, TMA>(w.y, w.z, d.rows, d.cols, d.planes, d.pos[parity], d.vel[parity],
+                                          d.force_in, d.pos[parity ^ 1], d.vel[parity ^ 1], c, wind, d.flags, mp, mv,
+                                          &bar, phase);
+    phase ^= TMA ? 1u : 0u;
     if (!persistent) break;
   }
 }
@@ -628,30 +629,52 @@ void batch_tiles(int cloth, int rows, int cols, int* out4, int* n_ring, int* n_i
     }
 }
 
+cudaError_t prime_step_kernels() {
+  static bool done = false;  // per process; the attribute is per function on the current device
+  if (done) return cudaSuccess;
+  const int smem = int(tiled_smem_bytes());
+  cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  done = e == cudaSuccess;
+  return e;
+}
+
 int batched_ctas_per_sm() {
   int n = 0;
   const size_t smem = tiled_smem_bytes();
-  cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_batched<kTileW, kTileH, kHalo>, kTileW * kTileH + kHalo,
-                                                    smem) != cudaSuccess)
+  cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_batched<kTileW, kTileH, kHalo, true>,
+                                                    kTileW * kTileH + kHalo, smem) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
 
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
-                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s, const void* maps) {
+                                int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s, const void* maps,
+                                const int* n_work_dev) {
   if (n_work <= 0) return cudaSuccess;
+  if (n_work_dev && mode != 1) return cudaErrorInvalidValue;  // a device count needs the persistent form
   const size_t smem = tiled_smem_bytes();
-  static bool attr_set = false;
-  if (!attr_set) {
-    const cudaError_t e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  const cudaError_t ea = prime_step_kernels();
+  if (ea != cudaSuccess) return ea;
   const int grid = mode == 1 ? (persistent_ctas < n_work ? persistent_ctas : n_work) : n_work;
-  k_step_batched<kTileW, kTileH, kHalo><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
-      cloths, work, n_work, counter, parity, mode == 1, c, static_cast<const CUtensorMap*>(maps));
+  const CUtensorMap* m = static_cast<const CUtensorMap*>(maps);
+  if (m)
+    k_step_batched<kTileW, kTileH, kHalo, true><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
+        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
+  else
+    k_step_batched<kTileW, kTileH, kHalo, false><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
+        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
   return cudaGetLastError();
 }
 
@@ -675,20 +698,19 @@ cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4*
     const int n_interior = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
     const int n_ring = t.tx * t.ty - n_interior;
     const size_t smem = tiled_smem_bytes();
-    static bool attr_set = false;  // per process; the attribute is per function on the current device
-    if (!attr_set) {
-      const cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
+    const cudaError_t ea = prime_step_kernels();
+    if (ea != cudaSuccess) return ea;
     CUtensorMap map_pos, map_vel;
     std::memset(&map_pos, 0, sizeof(map_pos));
     std::memset(&map_vel, 0, sizeof(map_vel));
-    const int use_tma =
-        encode_state_map(&map_pos, pos, g.rows, g.cols) && encode_state_map(&map_vel, vel, g.rows, g.cols) ? 1 : 0;
-    k_step_grid_tiled<kTileW, kTileH, kHalo><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
-        g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c, map_pos, map_vel, use_tma);
+    const bool use_tma =
+        encode_state_map(&map_pos, pos, g.rows, g.cols) && encode_state_map(&map_vel, vel, g.rows, g.cols);
+    if (use_tma)
+      k_step_grid_tiled<kTileW, kTileH, kHalo, true><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
+          g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c, map_pos, map_vel);
+    else
+      k_step_grid_tiled<kTileW, kTileH, kHalo, false><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
+          g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c, map_pos, map_vel);
   }
   return cudaGetLastError();
 }

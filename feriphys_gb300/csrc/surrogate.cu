@@ -45,49 +45,66 @@ __device__ __forceinline__ float2 unpack_bf2(uint32_t u) {
 // GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its
 // slope 0.5 (1 + t) + 0.5 x (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 x^2), with
 // the tanh argument as x (c + c a x^2) and explicit fused multiply-adds (this
-// file is compiled with -fmad=false).
+// file is compiled with -fmad=false).  Evaluated on pairs of columns with the
+// packed f32x2 operations (the same per-lane roundings as the scalar form).
 constexpr float kGeluCA = kGeluC * kGeluA;
 
-__device__ __forceinline__ float gelu(float x) {
-  const float u = __fmaf_rn(kGeluCA, x * x, kGeluC) * x;
-  const float t = tc::tanh_fast(u);
-  return x * __fmaf_rn(0.5f, t, 0.5f);
+using tc::f32x2;
+
+__device__ __forceinline__ f32x2 tanh2(f32x2 u) {
+  const float2 v = tc::f2_unpack(u);
+  return tc::f2_pack(tc::tanh_fast(v.x), tc::tanh_fast(v.y));
 }
 
-__device__ __forceinline__ void gelu_slope(float x, float& g, float& dg) {
-  const float x2 = x * x;
-  const float u = __fmaf_rn(kGeluCA, x2, kGeluC) * x;
-  const float t = tc::tanh_fast(u);
-  const float half1pt = __fmaf_rn(0.5f, t, 0.5f);
-  g = x * half1pt;
-  const float one_m_t2 = __fmaf_rn(-t, t, 1.0f);
-  const float du = __fmaf_rn(3.0f * kGeluCA, x2, kGeluC);
-  dg = __fmaf_rn((0.5f * x) * one_m_t2, du, half1pt);
+// GELU of the pair x, rounded to a bf16 pair.
+__device__ __forceinline__ uint32_t gelu2_bf(f32x2 x) {
+  const f32x2 u = tc::f2_mul(tc::f2_fma(tc::f2_splat(kGeluCA), tc::f2_mul(x, x), tc::f2_splat(kGeluC)), x);
+  const f32x2 t = tanh2(u);
+  const float2 h = tc::f2_unpack(tc::f2_mul(x, tc::f2_fma(tc::f2_splat(0.5f), t, tc::f2_splat(0.5f))));
+  return pack_bf2(h.x, h.y);
 }
 
-__device__ __forceinline__ void group_sync(int id) {
+// GELU and its slope of the pair x, each rounded to a bf16 pair.
+__device__ __forceinline__ void gelu2_slope_bf(f32x2 x, uint32_t& g, uint32_t& dg) {
+  const f32x2 x2 = tc::f2_mul(x, x);
+  const f32x2 u = tc::f2_mul(tc::f2_fma(tc::f2_splat(kGeluCA), x2, tc::f2_splat(kGeluC)), x);
+  const f32x2 t = tanh2(u);
+  const f32x2 half1pt = tc::f2_fma(tc::f2_splat(0.5f), t, tc::f2_splat(0.5f));
+  const float2 gv = tc::f2_unpack(tc::f2_mul(x, half1pt));
+  const f32x2 neg_t = tc::f2_mul(t, tc::f2_splat(-1.0f));  // exact
+  const f32x2 one_m_t2 = tc::f2_fma(neg_t, t, tc::f2_splat(1.0f));
+  const f32x2 du = tc::f2_fma(tc::f2_splat(3.0f * kGeluCA), x2, tc::f2_splat(kGeluC));
+  const f32x2 a = tc::f2_mul(tc::f2_mul(tc::f2_splat(0.5f), x), one_m_t2);
+  const float2 dv = tc::f2_unpack(tc::f2_fma(a, du, half1pt));
+  g = pack_bf2(gv.x, gv.y);
+  dg = pack_bf2(dv.x, dv.y);
+}
+
+// Barrier of one group of `n` threads (id 0: the whole CTA).
+__device__ __forceinline__ void group_sync(int id, int n = 128) {
   if (id == 0)
     __syncthreads();
   else
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(128) : "memory");
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
 // Generic-proxy writes and tensor-memory reads done by the group become
 // ordered before the MMA that one thread of the group issues next.
-__device__ __forceinline__ void sync_for_mma(int id) {
+__device__ __forceinline__ void sync_for_mma(int id, int n = 128) {
   tc::fence_before_sync();
   tc::fence_async_smem();
-  group_sync(id);
+  group_sync(id, n);
   tc::fence_after_sync();
 }
 
 // Bounded wait on an MMA/copy barrier by a whole group; every thread of the
 // group returns the same verdict.
-__device__ __forceinline__ bool group_wait(uint64_t* bar, uint32_t& phase, int id, volatile int* fail_flag) {
+__device__ __forceinline__ bool group_wait(uint64_t* bar, uint32_t& phase, int id, volatile int* fail_flag,
+                                           int n = 128) {
   const bool ok = tc::mbar_wait(bar, phase);
   phase ^= 1u;
   if (!ok) *fail_flag = 1;
-  group_sync(id);
+  group_sync(id, n);
   const bool all = *fail_flag == 0;
   tc::fence_after_sync();
   return all;
@@ -151,6 +168,91 @@ __device__ __forceinline__ void vertex_features(const SurCloth& c, int parity, i
   f[53] = atan2f(uz, ux) * kInvPi;
 }
 
+// The features of one row split over two threads: half 0 computes the
+// neighbours 0..3 and the pin and wind features (columns 0-11, 24-35,
+// 48-51), half 1 the neighbours 4..7 and the normal (columns 12-23, 36-47,
+// 52-53; 54-63 are zero); each writes its columns standardised, as bf16, into
+// the 64-wide tile.  Every feature is vertex_features' expression.
+template <int HALF>
+__device__ __forceinline__ void store_features_half(const SurCloth& c, int parity, int v, bool valid, const Norm& nm,
+                                                    unsigned char* X, int row) {
+  constexpr int NL = HALF == 0 ? 28 : 36;
+  float f[NL];
+#pragma unroll
+  for (int i = 0; i < NL; ++i) f[i] = 0.0f;
+  if (valid) {
+    const int R = c.rows, C = c.cols, r = v / C, col = v % C;
+    const float4* __restrict__ P = c.pos[parity];
+    const float4* __restrict__ Vl = c.vel[parity];
+    const float4* __restrict__ P0 = c.rest;
+    const float4 p = P[v], w0 = Vl[v], p0 = P0[v];
+    const float ih = c.inv_h, s = c.sv;
+    float3 q[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = 4 * HALF + j;
+      const int dr = k < 3 ? -1 : (k < 5 ? 0 : 1);
+      const int dc = (k == 0 || k == 3 || k == 5) ? -1 : ((k == 1 || k == 6) ? 0 : 1);
+      const int rr = r + dr, cc = col + dc;
+      q[j] = make_float3(p.x, p.y, p.z);
+      if (rr >= 0 && rr < R && cc >= 0 && cc < C) {
+        const int i = rr * C + cc;
+        const float4 a = P[i], w = Vl[i], a0 = P0[i];
+        q[j] = make_float3(a.x, a.y, a.z);
+        f[3 * j + 0] = ((a.x - p.x) - (a0.x - p0.x)) * ih;
+        f[3 * j + 1] = ((a.y - p.y) - (a0.y - p0.y)) * ih;
+        f[3 * j + 2] = ((a.z - p.z) - (a0.z - p0.z)) * ih;
+        f[12 + 3 * j + 0] = (w.x - w0.x) * s;
+        f[12 + 3 * j + 1] = (w.y - w0.y) * s;
+        f[12 + 3 * j + 2] = (w.z - w0.z) * s;
+      }
+    }
+    if (HALF == 0) {
+      f[24] = w0.w != 0.0f ? 1.0f : 0.0f;
+      f[25] = (c.wind[0] - w0.x) * s;
+      f[26] = (c.wind[1] - w0.y) * s;
+      f[27] = (c.wind[2] - w0.z) * s;
+    } else {
+      // neighbours 1 (up) and 3 (left) belong to the other half: load them here
+      float3 q1 = make_float3(p.x, p.y, p.z), q3 = q1;
+      if (r > 0) {
+        const float4 a = P[v - C];
+        q1 = make_float3(a.x, a.y, a.z);
+      }
+      if (col > 0) {
+        const float4 a = P[v - 1];
+        q3 = make_float3(a.x, a.y, a.z);
+      }
+      const float3 q4 = q[0], q6 = q[2];
+      const float ax = q4.x - q3.x, ay = q4.y - q3.y, az = q4.z - q3.z;
+      const float bx = q6.x - q1.x, by = q6.y - q1.y, bz = q6.z - q1.z;
+      const float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+      const float len = sqrtf((nx * nx + ny * ny) + nz * nz);
+      float ux = 0.0f, uy = 0.0f, uz = 1.0f;
+      if (len > 0.0f && isfinite(len)) {
+        const float il = 1.0f / len;
+        ux = nx * il;
+        uy = ny * il;
+        uz = nz * il;
+      }
+      f[24] = acosf(fminf(fmaxf(uy, -1.0f), 1.0f)) * kInvPi;
+      f[25] = atan2f(uz, ux) * kInvPi;
+    }
+  }
+#pragma unroll
+  for (int g4 = 0; g4 < NL / 4; ++g4) {
+    const int li = 4 * g4;
+    const int col = li < 12 ? 12 * HALF + li : (li < 24 ? 24 + 12 * HALF + (li - 12) : 48 + 4 * HALF + (li - 24));
+    float x[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int k = col + e < kFeat ? col + e : 0;
+      x[e] = (valid && col + e < kFeat) ? (f[li + e] - nm.in_mean[k]) * nm.in_inv_std[k] : 0.0f;
+    }
+    *reinterpret_cast<uint2*>(X + tc::blk_off(kIn, row, col)) = make_uint2(pack_bf2(x[0], x[1]), pack_bf2(x[2], x[3]));
+  }
+}
+
 // Standardised features of row `lt` as bf16 into a 64-wide blocked tile.
 __device__ __forceinline__ void store_input_row(unsigned char* X, int lt, const float (&f)[kFeat], bool valid,
                                                 const Norm& nm) {
@@ -174,12 +276,13 @@ __device__ __forceinline__ void store_input_row(unsigned char* X, int lt, const 
 
 // ---- network stages --------------------------------------------------------
 
-// z (TMEM lane = this thread's row, 128 columns) + bias -> GELU -> bf16 row of
-// the 128-wide tile H; with G != null also the GELU slope into G.
+// z (TMEM lane = this thread's row, columns [c0, c1)) + bias -> GELU -> bf16
+// row of the 128-wide tile H; with G != null also the GELU slope into G.
 __device__ __forceinline__ void epilogue_gelu(uint32_t taddr, const float* __restrict__ bias, unsigned char* H,
-                                              unsigned char* G, int lt) {
+                                              unsigned char* G, int lt, int c0 = 0, int c1 = kHid) {
+  const f32x2* __restrict__ bias2 = reinterpret_cast<const f32x2*>(bias);
 #pragma unroll 1
-  for (int cb = 0; cb < kHid; cb += 32) {
+  for (int cb = c0; cb < c1; cb += 32) {
     float z[32];
     tc::tmem_ld32(taddr + cb, z);
 #pragma unroll
@@ -188,15 +291,11 @@ __device__ __forceinline__ void epilogue_gelu(uint32_t taddr, const float* __res
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int a = 8 * q + 2 * j;
-        if (G) {
-          float h0, d0, h1, d1;
-          gelu_slope(z[a] + bias[cb + a], h0, d0);
-          gelu_slope(z[a + 1] + bias[cb + a + 1], h1, d1);
-          uh[j] = pack_bf2(h0, h1);
-          ug[j] = pack_bf2(d0, d1);
-        } else {
-          uh[j] = pack_bf2(gelu(z[a] + bias[cb + a]), gelu(z[a + 1] + bias[cb + a + 1]));
-        }
+        const f32x2 x = tc::f2_add(tc::f2_pack(z[a], z[a + 1]), bias2[(cb + a) >> 1]);
+        if (G)
+          gelu2_slope_bf(x, uh[j], ug[j]);
+        else
+          uh[j] = gelu2_bf(x);
       }
       const uint32_t off = tc::blk_off(kHid, lt, cb + 8 * q);
       *reinterpret_cast<uint4*>(H + off) = make_uint4(uh[0], uh[1], uh[2], uh[3]);
@@ -220,7 +319,9 @@ __device__ __forceinline__ void epilogue_backward(uint32_t taddr, unsigned char*
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const float2 g = unpack_bf2(gw[j]);
-        o[j] = pack_bf2(d[8 * q + 2 * j] * g.x, d[8 * q + 2 * j + 1] * g.y);
+        const float2 p = tc::f2_unpack(
+            tc::f2_mul(tc::f2_pack(d[8 * q + 2 * j], d[8 * q + 2 * j + 1]), tc::f2_pack(g.x, g.y)));
+        o[j] = pack_bf2(p.x, p.y);
       }
       *reinterpret_cast<uint4*>(G + off) = make_uint4(o[0], o[1], o[2], o[3]);
     }
@@ -228,11 +329,16 @@ __device__ __forceinline__ void epilogue_backward(uint32_t taddr, unsigned char*
 }
 
 // The three layers for the tile in `act` (inputs in the 64-wide layout on
-// entry; the hidden activations overwrite it).  Returns the thread's row of
-// the 16 output columns with the bias added.
+// entry; the hidden activations overwrite it), run by a group of 128 * H
+// threads: thread lt of the group owns row lt % 128 and the hidden columns
+// [64 h, 64 h + 128 / H) with h = lt / 128.  The threads of h = 0 return their
+// row of the 16 output columns with the bias added in y.
+template <int H>
 __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char* wsm, uint32_t tmem,
                                          uint32_t lane_off, uint64_t* bar, uint32_t& phase, int lt, int bar_id,
                                          volatile int* fail_flag, float (&y)[16]) {
+  constexpr int NT = 128 * H, NC = kHid / H;
+  const int row = lt & 127, c0 = (lt >> 7) * NC;
   const uint32_t a_act = tc::smem_u32(act);
   const uint32_t a_w1 = tc::smem_u32(wsm + kBlobW1), a_w2 = tc::smem_u32(wsm + kBlobW2),
                  a_w3 = tc::smem_u32(wsm + kBlobW3);
@@ -241,7 +347,7 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char
   const float* b3 = reinterpret_cast<const float*>(wsm + kBlobB3);
   constexpr uint32_t id_hid = tc::idesc_bf16(128, kHid), id_out = tc::idesc_bf16(128, kOutPad);
 
-  sync_for_mma(bar_id);
+  sync_for_mma(bar_id, NT);
   if (lt == 0) {
 #pragma unroll
     for (int s = 0; s < kIn / 16; ++s)
@@ -249,10 +355,10 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char
                    s > 0);
     tc::mma_commit(bar);
   }
-  if (!group_wait(bar, phase, bar_id, fail_flag)) return false;
-  epilogue_gelu(tmem + lane_off, b1, act, nullptr, lt);
+  if (!group_wait(bar, phase, bar_id, fail_flag, NT)) return false;
+  epilogue_gelu(tmem + lane_off, b1, act, nullptr, row, c0, c0 + NC);
 
-  sync_for_mma(bar_id);
+  sync_for_mma(bar_id, NT);
   if (lt == 0) {
 #pragma unroll
     for (int s = 0; s < kHid / 16; ++s)
@@ -260,10 +366,10 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char
                    id_hid, s > 0);
     tc::mma_commit(bar);
   }
-  if (!group_wait(bar, phase, bar_id, fail_flag)) return false;
-  epilogue_gelu(tmem + lane_off, b2, act, nullptr, lt);
+  if (!group_wait(bar, phase, bar_id, fail_flag, NT)) return false;
+  epilogue_gelu(tmem + lane_off, b2, act, nullptr, row, c0, c0 + NC);
 
-  sync_for_mma(bar_id);
+  sync_for_mma(bar_id, NT);
   if (lt == 0) {
 #pragma unroll
     for (int s = 0; s < kHid / 16; ++s)
@@ -271,27 +377,35 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char
                    id_out, s > 0);
     tc::mma_commit(bar);
   }
-  if (!group_wait(bar, phase, bar_id, fail_flag)) return false;
-  tc::tmem_ld16(tmem + lane_off, y);
+  if (!group_wait(bar, phase, bar_id, fail_flag, NT)) return false;
+  if (lt < 128) {  // warp-uniform
+    tc::tmem_ld16(tmem + lane_off, y);
 #pragma unroll
-  for (int j = 0; j < 16; ++j) y[j] += b3[j];
+    for (int j = 0; j < 16; ++j) y[j] += b3[j];
+  }
   return true;
 }
 
 // ---- inference: the coarse step --------------------------------------------
 
-template <int G>
-__global__ void __launch_bounds__(128 * G, 1)
+// G groups of 128 * H threads; a group takes one 128-vertex tile at a time,
+// H threads per vertex row (H = 2: each computes half of the row's features
+// and half of its hidden columns, so twice the warps hide the latencies).
+template <int G, int H>
+__global__ void __launch_bounds__(128 * G * H, 1)
     k_sur_step(const SurCloth* __restrict__ cloths, const Tile* __restrict__ tiles, int n_tiles, int parity,
                const unsigned char* __restrict__ blob, const Norm norm, const StepConsts cst, int* err) {
+  static_assert(H == 1 || H == 2, "one or two threads per row");
+  constexpr int NT = 128 * H;
+  constexpr uint32_t kCols = G == 1 ? 128 : (G == 2 ? 256 : 512);  // a power of two >= 128 G
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint64_t bar_w;
   __shared__ uint64_t bar_g[G];
   __shared__ uint32_t tslot;
   __shared__ int gfail[G];
-  const int tid = threadIdx.x, g = tid >> 7, lt = tid & 127;
+  const int tid = threadIdx.x, g = tid / NT, lt = tid % NT, row = lt & 127;
   if (tid < 32) {
-    tc::tmem_alloc(&tslot, 128 * G);
+    tc::tmem_alloc(&tslot, kCols);
     tc::tmem_relinquish();
     tc::fence_before_sync();
   }
@@ -309,7 +423,7 @@ __global__ void __launch_bounds__(128 * G, 1)
   }
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0)) != 0;
   const uint32_t tmem = tslot + uint32_t(g * 128);
-  const uint32_t lane_off = uint32_t((lt >> 5) * 32) << 16;
+  const uint32_t lane_off = uint32_t((row >> 5) * 32) << 16;
   unsigned char* act = smem + kBlobSmem + g * 32768;
   const ObsFace* faces = static_cast<const ObsFace*>(cst.obstacle_faces);
   uint32_t phase = 0;
@@ -317,17 +431,21 @@ __global__ void __launch_bounds__(128 * G, 1)
     const Tile w = tiles[t];
     const SurCloth& c = cloths[w.x];
     const int n = c.rows * c.cols;
-    const int v = w.y + lt;
+    const int v = w.y + row;
     const bool valid = v < n;
-    {
+    if (H == 1) {
       float f[kFeat];
       if (valid) vertex_features(c, parity, v / c.cols, v % c.cols, f);
-      store_input_row(act, lt, f, valid, norm);
+      store_input_row(act, row, f, valid, norm);
+    } else if (lt < 128) {  // warp-uniform
+      store_features_half<0>(c, parity, v, valid, norm, act, row);
+    } else {
+      store_features_half<1>(c, parity, v, valid, norm, act, row);
     }
     float y[16];
-    ok = mlp_tile(act, smem, tmem, lane_off, &bar_g[g], phase, lt, 1 + g, &gfail[g], y);
+    ok = mlp_tile<H>(act, smem, tmem, lane_off, &bar_g[g], phase, lt, 1 + g, &gfail[g], y);
     if (!ok) break;
-    if (valid) {
+    if (valid && lt < 128) {
       const float4 P = c.pos[parity][v], V = c.vel[parity][v];
       float4 PO = P, VO = V;
       if (V.w == 0.0f) {
@@ -355,7 +473,7 @@ __global__ void __launch_bounds__(128 * G, 1)
   __syncthreads();
   if (tid < 32) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(tslot, 128 * G);
+    tc::tmem_dealloc(tslot, kCols);
   }
 }
 
@@ -399,7 +517,7 @@ __global__ void __launch_bounds__(128, 1)
     ok = group_wait(&bar_x, ph_x, 0, &fail);
     if (!ok) break;
     float y[16];
-    ok = mlp_tile(act, smem, tmem, lane_off, &bar_m, ph_m, lt, 0, &fail, y);
+    ok = mlp_tile<1>(act, smem, tmem, lane_off, &bar_m, ph_m, lt, 0, &fail, y);
     if (!ok) break;
     reinterpret_cast<float4*>(Y)[size_t(t) * 128 + lt] = make_float4(y[0], y[1], y[2], 0.0f);
     tc::fence_before_sync();
@@ -827,11 +945,6 @@ __global__ void k_stats(const float* __restrict__ feat, const float* __restrict_
 
 // ---- checks ----------------------------------------------------------------
 
-__device__ __forceinline__ float plane_val(const float4* planes, int n, int v, int idx) {
-  const float* pl = reinterpret_cast<const float*>(planes + size_t(idx >> 2) * n);
-  return pl[4 * size_t(v) + (idx & 3)];
-}
-
 __global__ void __launch_bounds__(128) k_check(const SurCloth* __restrict__ cloths, const Tile* __restrict__ tiles,
                                                int n_tiles, int parity, float3 gf, float2* __restrict__ tile_out) {
   __shared__ float2 red[4];
@@ -847,6 +960,20 @@ __global__ void __launch_bounds__(128) k_check(const SurCloth* __restrict__ clot
   if (v < n) {
     const int r = v / C, col = v % C;
     const float4 p = P[v], vel = Vl[v];
+    // the vertex's owned-strut constants: one row of each of the four planes
+    float prm[16];
+    {
+      const float4 q0 = c.planes[v], q1 = c.planes[size_t(n) + v], q2 = c.planes[2 * size_t(n) + v],
+                   q3 = c.planes[3 * size_t(n) + v];
+      const float4 q[4] = {q0, q1, q2, q3};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        prm[4 * j] = q[j].x;
+        prm[4 * j + 1] = q[j].y;
+        prm[4 * j + 2] = q[j].z;
+        prm[4 * j + 3] = q[j].w;
+      }
+    }
     E = 0.5f * p.w * ((vel.x * vel.x + vel.y * vel.y) + vel.z * vel.z) - ((gf.x * p.x + gf.y * p.y) + gf.z * p.z);
 #pragma unroll
     for (int kind = 0; kind < 5; ++kind) {
@@ -859,11 +986,11 @@ __global__ void __launch_bounds__(128) k_check(const SurCloth* __restrict__ clot
         case grid::KBH: b = v + 2; break;
         default: b = v + 2 * C; break;
       }
-      const float4 pa = P[a], pb = P[b];
+      const float4 pa = a == v ? p : P[a], pb = P[b];
       const float dx = pb.x - pa.x, dy = pb.y - pa.y, dz = pb.z - pa.z;
       const float d = sqrtf((dx * dx + dy * dy) + dz * dz);
-      const float k = plane_val(c.planes, n, v, grid::param_index(kind, 0));
-      const float L = plane_val(c.planes, n, v, grid::param_index(kind, 2));
+      const float k = prm[grid::param_index(kind, 0)];
+      const float L = prm[grid::param_index(kind, 2)];
       const float e = d - L;
       E += 0.5f * k * (e * e);
       S = fmaxf(S, fabsf(e / L));
@@ -882,24 +1009,34 @@ __global__ void __launch_bounds__(128) k_check(const SurCloth* __restrict__ clot
                               fmaxf(fmaxf(red[0].y, red[1].y), fmaxf(red[2].y, red[3].y)));
 }
 
-// One warp per cloth: sums (and maxima) of its tiles' entries, strided by
-// lane then combined by shuffles, in a fixed order.
-__global__ void k_check_reduce(const SurCloth* __restrict__ cloths, int n_cloths, const float2* __restrict__ tile_out,
-                               float2* __restrict__ cloth_out) {
-  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (c >= n_cloths) return;
+// One block per cloth: sums (and maxima) of its tiles' entries, strided by
+// thread, then a fixed-order tree over the block (the same order on every
+// run, whatever the number of tiles).
+constexpr int kReduceBlock = 256;
+
+__global__ void __launch_bounds__(kReduceBlock) k_check_reduce(const SurCloth* __restrict__ cloths,
+                                                               const float2* __restrict__ tile_out,
+                                                               float2* __restrict__ cloth_out) {
+  __shared__ float2 sh[kReduceBlock];
+  const int c = blockIdx.x;
   const SurCloth& cl = cloths[c];
   float E = 0.0f, S = 0.0f;
-  for (int k = lane; k < cl.ntiles; k += 32) {
+  for (int k = threadIdx.x; k < cl.ntiles; k += kReduceBlock) {
     const float2 e = tile_out[cl.tile0 + k];
     E += e.x;
     S = fmaxf(S, e.y);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    E += __shfl_xor_sync(0xffffffffu, E, o);
-    S = fmaxf(S, __shfl_xor_sync(0xffffffffu, S, o));
+  sh[threadIdx.x] = make_float2(E, S);
+  __syncthreads();
+#pragma unroll
+  for (int h = kReduceBlock / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      const float2 a = sh[threadIdx.x], b = sh[threadIdx.x + h];
+      sh[threadIdx.x] = make_float2(a.x + b.x, fmaxf(a.y, b.y));
+    }
+    __syncthreads();
   }
-  if (lane == 0) cloth_out[c] = make_float2(E, S);
+  if (threadIdx.x == 0) cloth_out[c] = sh[0];
 }
 
 __global__ void k_copy_unskipped(const ClothDesc* __restrict__ cloths, int from) {
@@ -910,6 +1047,113 @@ __global__ void k_copy_unskipped(const ClothDesc* __restrict__ cloths, int from)
     d.pos[from ^ 1][i] = d.pos[from][i];
     d.vel[from ^ 1][i] = d.vel[from][i];
   }
+}
+
+// ---- device-side decisions of a checked rollout ------------------------------
+
+// Per cloth: the rollout's energy/strain test of the state a coarse step
+// produced (cloth_out) against the last accepted energy e_old and the margin
+// growth * e_ref + abs, evaluated in double exactly as the host form does.
+// Passing cloths accept their new energy; fail[c] is the verdict; n_fail
+// counts this step's failures.
+__global__ void k_decide(const float2* __restrict__ cloth_out, int n_cloths, float* __restrict__ e_old,
+                         const double* __restrict__ e_ref, float growth, float abs_margin, float max_strain,
+                         int* __restrict__ fail, int* __restrict__ n_fail) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cloths) return;
+  const float2 o = cloth_out[c];
+  const double E0 = e_old[c], E1 = o.x, S1 = o.y;
+  const double margin = double(growth) * e_ref[c] + double(abs_margin);
+  const bool ok = isfinite(E1) && isfinite(S1) && (E1 <= E0 + margin) && (S1 <= double(max_strain));
+  fail[c] = ok ? 0 : 1;
+  if (ok)
+    e_old[c] = o.x;
+  else
+    atomicAdd(n_fail, 1);
+}
+
+// One thread: the graph's fallback conditional from this step's failure
+// count, which is also added to the call's running total.
+__global__ void k_set_fallback(cudaGraphConditionalHandle h, const int* __restrict__ n_fail,
+                               unsigned long long* __restrict__ total) {
+  const int v = *n_fail;
+  cudaGraphSetConditional(h, v > 0 ? 1u : 0u);
+  *total += (unsigned long long)v;
+}
+
+// The batched fallback's cloth table (the batch's, with skip = !fail and no
+// carried forces) and, for each failing cloth, where its work items go in the
+// compacted list (an exclusive scan in batch order, so the compacted list
+// keeps the full list's order); the item count goes to *n_out.  One block.
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) k_fallback_tables(const ClothDesc* __restrict__ desc,
+                                                                const int* __restrict__ bmesh, int n_batch,
+                                                                const int* __restrict__ fail,
+                                                                const int* __restrict__ cnt,
+                                                                ClothDesc* __restrict__ fdesc,
+                                                                int* __restrict__ dst, int* __restrict__ n_out) {
+  __shared__ int warp_sum[kScanBlock / 32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < n_batch; b0 += kScanBlock) {
+    const int b = b0 + threadIdx.x;
+    int m = 0;
+    if (b < n_batch) {
+      const int f = fail[bmesh[b]];
+      ClothDesc d = desc[b];
+      d.skip = f ? 0 : 1;
+      d.force_in = nullptr;
+      fdesc[b] = d;
+      m = f ? cnt[b] : 0;
+    }
+    int x = m;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int w = warp_sum[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_sum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = carry + (wid > 0 ? warp_sum[wid - 1] : 0) + x - m;
+    if (b < n_batch) dst[b] = before;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1) carry = before + m;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *n_out = carry;
+}
+
+// One block per cloth of the batch: a failing cloth's work items
+// [off, off + cnt) of the full list, copied to [dst, dst + cnt).
+__global__ void k_fallback_items(const int* __restrict__ bmesh, const int* __restrict__ fail,
+                                 const int* __restrict__ off, const int* __restrict__ cnt,
+                                 const int* __restrict__ dst, const int4* __restrict__ work,
+                                 int4* __restrict__ fwork) {
+  const int b = blockIdx.x;
+  if (!fail[bmesh[b]]) return;
+  const int o = off[b], n = cnt[b], d = dst[b];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) fwork[d + i] = work[o + i];
+}
+
+// After a fallback: the re-checked energy of every cloth that fell back
+// becomes its accepted energy.
+__global__ void k_accept(const float2* __restrict__ cloth_out, int n_cloths, const int* __restrict__ fail,
+                         float* __restrict__ e_old) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n_cloths && fail[c]) e_old[c] = cloth_out[c].x;
 }
 
 int g_sms = 0;
@@ -924,33 +1168,58 @@ int sm_count() {
   return g_sms;
 }
 
-template <int G>
+template <int G, int H>
+cudaError_t sur_step_attr() {
+  static bool done = false;  // per process; the attribute is per function on the current device
+  if (done) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_sur_step<G, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBlobSmem + G * 32768);
+  done = e == cudaSuccess;
+  return e;
+}
+
+template <int G, int H>
 cudaError_t sur_step_g(const SurCloth* cloths, const Tile* tiles, int n_tiles, int parity, const void* blob,
                        const Norm& norm, const StepConsts& consts, int ctas, int* err, cudaStream_t s) {
   const int smem = kBlobSmem + G * 32768;
-  cudaError_t e = cudaFuncSetAttribute(k_sur_step<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const cudaError_t e = sur_step_attr<G, H>();
   if (e != cudaSuccess) return e;
   int grid = (n_tiles + G - 1) / G;
   const int cap = ctas > 0 ? ctas : sm_count();
   if (grid > cap) grid = cap;
   if (grid < 1) return cudaSuccess;
-  k_sur_step<G><<<grid, 128 * G, smem, s>>>(cloths, tiles, n_tiles, parity, static_cast<const unsigned char*>(blob),
-                                            norm, consts, err);
+  k_sur_step<G, H><<<grid, 128 * G * H, smem, s>>>(cloths, tiles, n_tiles, parity,
+                                                   static_cast<const unsigned char*>(blob), norm, consts, err);
   return cudaGetLastError();
 }
 
 }  // namespace
 
+// Threads per vertex row in k_sur_step.
+constexpr int kRowThreads = 2;
+
 int sur_step_max_ctas(int) { return sm_count(); }
+
+cudaError_t prime_sur_step(int groups) {
+  switch (groups) {
+    case 1: return sur_step_attr<1, kRowThreads>();
+    case 2: return sur_step_attr<2, kRowThreads>();
+    case 3: return sur_step_attr<3, kRowThreads>();
+    default: return sur_step_attr<4, kRowThreads>();
+  }
+}
+
+
 
 cudaError_t launch_sur_step(const SurCloth* cloths, const Tile* tiles, int n_tiles, int parity, const void* blob,
                             const Norm& norm, const StepConsts& consts, int groups, int ctas, int* err,
                             cudaStream_t s) {
   if (n_tiles <= 0) return cudaSuccess;
   switch (groups) {
-    case 1: return sur_step_g<1>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
-    case 2: return sur_step_g<2>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
-    default: return sur_step_g<4>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
+    case 1: return sur_step_g<1, kRowThreads>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
+    case 2: return sur_step_g<2, kRowThreads>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
+    case 3: return sur_step_g<3, kRowThreads>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
+    default: return sur_step_g<4, kRowThreads>(cloths, tiles, n_tiles, parity, blob, norm, consts, ctas, err, s);
   }
 }
 
@@ -1047,7 +1316,36 @@ cudaError_t launch_check(const SurCloth* cloths, const Tile* tiles, int n_tiles,
                          float3 gforce, float2* tile_out, float2* cloth_out, cudaStream_t s) {
   if (n_tiles <= 0) return cudaSuccess;
   k_check<<<n_tiles, kTile, 0, s>>>(cloths, tiles, n_tiles, parity, gforce, tile_out);
-  k_check_reduce<<<(n_cloths * 32 + 255) / 256, 256, 0, s>>>(cloths, n_cloths, tile_out, cloth_out);
+  if (n_cloths > 0) k_check_reduce<<<n_cloths, kReduceBlock, 0, s>>>(cloths, tile_out, cloth_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_decide(const float2* cloth_out, int n_cloths, float* e_old, const double* e_ref, float growth,
+                          float abs_margin, float max_strain, int* fail, int* n_fail, cudaStream_t s) {
+  if (n_cloths <= 0) return cudaSuccess;
+  k_decide<<<(n_cloths + 255) / 256, 256, 0, s>>>(cloth_out, n_cloths, e_old, e_ref, growth, abs_margin, max_strain,
+                                                  fail, n_fail);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_fallback(cudaGraphConditionalHandle h, const int* n_fail, unsigned long long* total,
+                                cudaStream_t s) {
+  k_set_fallback<<<1, 1, 0, s>>>(h, n_fail, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fallback_tables(const ClothDesc* desc, const int* bmesh, int n_batch, const int* fail,
+                                   const int* off, const int* cnt, const int4* work, ClothDesc* fdesc, int* dst,
+                                   int4* fwork, int* n_out, cudaStream_t s) {
+  if (n_batch <= 0) return cudaSuccess;
+  k_fallback_tables<<<1, kScanBlock, 0, s>>>(desc, bmesh, n_batch, fail, cnt, fdesc, dst, n_out);
+  k_fallback_items<<<n_batch, 128, 0, s>>>(bmesh, fail, off, cnt, dst, work, fwork);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accept(const float2* cloth_out, int n_cloths, const int* fail, float* e_old, cudaStream_t s) {
+  if (n_cloths <= 0) return cudaSuccess;
+  k_accept<<<(n_cloths + 255) / 256, 256, 0, s>>>(cloth_out, n_cloths, fail, e_old);
   return cudaGetLastError();
 }
 

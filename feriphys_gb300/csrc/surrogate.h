@@ -148,7 +148,7 @@ cudaError_t launch_stats(const float* feat, const float* tgt, long long count, d
 // Energy and maximum strain of each cloth's state in buffers [parity]:
 // E = sum (m |v|^2 / 2 - g . p) + sum over struts k (|d| - L)^2 / 2,
 // strain = max |(|d| - L) / L|; g is the gravity force of a point.  One entry
-// per tile (warp-shuffle sums), then one per cloth (a warp sums the cloth's
+// per tile (warp-shuffle sums), then one per cloth (a block sums the cloth's
 // tiles in a fixed order): cloth_out[c] = {E, strain}.
 cudaError_t launch_check(const SurCloth* cloths, const Tile* tiles, int n_tiles, int n_cloths, int parity,
                          float3 gforce, float2* tile_out, float2* cloth_out, cudaStream_t s);
@@ -157,6 +157,30 @@ cudaError_t launch_check(const SurCloth* cloths, const Tile* tiles, int n_tiles,
 // state from buffers [from] to [from ^ 1] (the fine-step fallback restores
 // the pre-step state before stepping from it).
 cudaError_t launch_copy_unskipped(const ClothDesc* cloths, int n_cloths, int from, cudaStream_t s);
+
+// Device-side decisions of a checked rollout (no host round trip per coarse
+// step).  launch_decide: per cloth, the energy/strain test of cloth_out
+// against e_old and the margin growth * e_ref + abs (in double, as the host
+// form), fail[c] = verdict, e_old[c] = E for passing cloths, n_fail += the
+// failures.  launch_set_fallback: one thread sets the graph conditional h to
+// (*n_fail > 0) and adds *n_fail to *total.  launch_fallback_tables: the
+// batched fallback's cloth table (skip = !fail[bmesh[b]], no forces) and the
+// failing cloths' work items (cloth b owns items [off[b], off[b] + cnt[b])
+// of `work`) compacted in list order into fwork, their count in *n_out
+// (dst: n_batch ints of scratch).  launch_accept: e_old[c] = cloth_out[c].x
+// for every failing cloth.
+cudaError_t launch_decide(const float2* cloth_out, int n_cloths, float* e_old, const double* e_ref, float growth,
+                          float abs_margin, float max_strain, int* fail, int* n_fail, cudaStream_t s);
+cudaError_t launch_set_fallback(cudaGraphConditionalHandle h, const int* n_fail, unsigned long long* total,
+                                cudaStream_t s);
+cudaError_t launch_fallback_tables(const ClothDesc* desc, const int* bmesh, int n_batch, const int* fail,
+                                   const int* off, const int* cnt, const int4* work, ClothDesc* fdesc, int* dst,
+                                   int4* fwork, int* n_out, cudaStream_t s);
+cudaError_t launch_accept(const float2* cloth_out, int n_cloths, const int* fail, float* e_old, cudaStream_t s);
+
+// Sets the launch attributes of the coarse-step kernels (call before a
+// stream capture that launches them).
+cudaError_t prime_sur_step(int groups);
 
 }  // namespace sur
 }  // namespace fgb

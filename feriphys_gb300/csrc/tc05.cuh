@@ -192,5 +192,43 @@ __device__ __forceinline__ float tanh_fast(float x) {
   return y;
 }
 
+// Packed pairs of f32 in one 64-bit register (PTX .f32x2, sm_100 and later):
+// one add/mul/fma instruction does both lanes, each lane rounded exactly as
+// the scalar .rn operation, so a sequence of packed operations gives the same
+// bits as the scalar sequence it replaces.
+using f32x2 = unsigned long long;
+
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+
+__device__ __forceinline__ float2 f2_unpack(f32x2 r) {
+  float2 v;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+  return v;
+}
+
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+__device__ __forceinline__ f32x2 f2_splat(float a) { return f2_pack(a, a); }
+
 }  // namespace tc
 }  // namespace fgb

@@ -230,6 +230,49 @@ def test_batched_fallback_reverts_every_failing_cloth():
         assert np.array_equal(a.get_points(), b.get_points())
 
 
+def _rollout(build, sur, ratio, steps, chk, graphs):
+    sim, meshes = build()
+    sim.set_graphs(graphs)
+    n = sim.step_surrogate(sur, ratio, steps, chk)
+    return n, [m.get_points() for m in meshes]
+
+
+@pytest.mark.parametrize("kind", ["single", "batch"])
+def test_device_decisions_equal_host_decisions(kind):
+    """The checked rollout decided on the device (one graph per coarse step,
+    the fallback under a conditional node, no host wait between steps) gives
+    the host-decided loop's verdicts: equal fallback counts and bit-identical
+    states, with the network's outputs scaled from harmless to wild so that
+    some steps (and, in a batch, some cloths) fall back and others do not;
+    even and odd ratios (with and without the restoring copy)."""
+    steps = 6
+    if kind == "single":
+        def build():
+            _, sim, mesh, _ = small_scene()
+            return sim, [mesh]
+        cap = steps
+    else:
+        batch = W.c2(n_cloths=6, lo=12, hi=70, seed=5, dt=1.0 / 6000.0)
+
+        def build():
+            sim, meshes, _ = W.build_batch(batch, fgb)
+            return sim, meshes
+        cap = 6 * steps
+    sur = fgb.Surrogate.new(21)
+    chk = fgb.SurrogateCheck.make(energy_growth=1e-3, energy_abs=1e-7, max_strain=0.5)
+    counts = []
+    for scale in (1e-4, *np.geomspace(1e-2, 1e-1, 9), 100.0):
+        sur.set_normalization(np.zeros(54), np.ones(54), np.zeros(3), np.full(3, scale))
+        for ratio in (10, 3):
+            n_dev, p_dev = _rollout(build, sur, ratio, steps, chk, True)
+            n_host, p_host = _rollout(build, sur, ratio, steps, chk, False)
+            assert n_dev == n_host, (scale, ratio)
+            for a, b in zip(p_dev, p_host):
+                assert np.array_equal(a, b), (scale, ratio)
+            counts.append(n_dev)
+    assert any(0 < c < cap for c in counts), counts
+
+
 def test_energy_matches_numpy():
     sc, sim, mesh, _ = small_scene()
     sim.step(20)
