@@ -61,10 +61,11 @@ __device__ __forceinline__ MassDiv mass_div(float m) {
   const bool fast = rcp_usable(m);
   return {m, fast ? __frcp_rn(m) : 0.0f, fast};
 }
+static __device__ __noinline__ V3<float> div3_ieee_cold(V3<float> F, float m) { return F / m; }
 __device__ __forceinline__ V3<float> div_mass(V3<float> F, float m, const MassDiv& d) {
   if (d.fast && m == d.m && !signbit(m) == !signbit(d.m))
     return {div_known_rcp(F.x, d.m, d.y), div_known_rcp(F.y, d.m, d.y), div_known_rcp(F.z, d.m, d.y)};
-  return F / m;
+  return div3_ieee_cold(F, m);
 }
 struct MassDivD {
   double m;
@@ -72,19 +73,20 @@ struct MassDivD {
 __device__ __forceinline__ MassDivD mass_div(double m) { return {m}; }
 __device__ __forceinline__ V3<double> div_mass(V3<double> F, double m, const MassDivD&) { return F / m; }
 
-// State integration of one point with frozen force F.  m' = m + 0*h and
-// F' = F + 0*h are kept (they only differ from m, F in the sign of zero).
 template <class T>
-__device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V3<T> v, V3<T> F, T m, V3<T>& np,
-                                                V3<T>& nv, V3<T>& nF) {
+struct Integrated {
+  V3<T> p, v, F;
+};
+
+// state.rs:86-106: k1..k4 share the carried F, so only the v stages differ.
+// Out of line: the Euler step is the common case and this branch, inlined,
+// doubled the integration code of every step kernel.
+template <class T>
+static __device__ __noinline__ Integrated<T> integrate_rk4(T h, V3<T> p, V3<T> v, V3<T> F, T m) {
   const V3<T> z3{T(0), T(0), T(0)};
   const auto md = mass_div(m);
-  if (integration == 0) {  // state.rs:75-83
-    const V3<T> a = div_mass(F, m, md);
-    np = p + v * h;
-    nv = v + a * h;
-    nF = F + z3 * h;
-  } else {  // state.rs:86-106: k1..k4 share the carried F, so only v stages differ
+  Integrated<T> out;
+  {
     const T hh = h * T(0.5);
     const V3<T> a1 = div_mass(F, m, md);
     const V3<T> F2 = F + z3 * hh;
@@ -100,10 +102,30 @@ __device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V
     const V3<T> v4 = v + a3 * h;
     const V3<T> a4 = div_mass(F4, m4, md);
     const T h6 = h / T(6), h3 = h / T(3);
-    np = p + (((h6 * v + h3 * v2) + h3 * v3) + h6 * v4);
-    nv = v + (((h6 * a1 + h3 * a2) + h3 * a3) + h6 * a4);
+    out.p = p + (((h6 * v + h3 * v2) + h3 * v3) + h6 * v4);
+    out.v = v + (((h6 * a1 + h3 * a2) + h3 * a3) + h6 * a4);
     const V3<T> zf = ((h6 * z3 + h3 * z3) + h3 * z3) + h6 * z3;
-    nF = F + zf;
+    out.F = F + zf;
+  }
+  return out;
+}
+
+// State integration of one point with frozen force F.  m' = m + 0*h and
+// F' = F + 0*h are kept (they only differ from m, F in the sign of zero).
+template <class T>
+__device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V3<T> v, V3<T> F, T m, V3<T>& np,
+                                                V3<T>& nv, V3<T>& nF) {
+  if (integration == 0) {  // state.rs:75-83
+    const V3<T> z3{T(0), T(0), T(0)};
+    const V3<T> a = div_mass(F, m, mass_div(m));
+    np = p + v * h;
+    nv = v + a * h;
+    nF = F + z3 * h;
+  } else {
+    const Integrated<T> r = integrate_rk4<T>(h, p, v, F, m);
+    np = r.p;
+    nv = r.v;
+    nF = r.F;
   }
 }
 
@@ -202,14 +224,16 @@ __device__ __forceinline__ bool test_faces_from(const ObsFace* __restrict__ face
 // First hit with the broad phase: obstacles in order; within one, the faces
 // of the query's cell merged with the always-tested faces in ascending
 // index.  The narrow test is the same face_hit as the full search, so the
-// result is identical.
+// result is identical.  Every candidate -- a linear range of faces (no
+// broad phase, or a query box that fits no cell) or the merge of two sorted
+// lists -- goes through one face_hit site, and the response is applied once
+// after the search: the inlined code stays small.
 template <class T>
 __device__ __forceinline__ bool collide_point(const ObsFace* __restrict__ faces, int n_faces, V3<T> op, V3<T> ov,
                                               V3<T> oF, T om, V3<T>& np, V3<T>& nv, const StepConsts& c) {
   if (n_faces == 0) return false;
   const ObsAccel& A = c.accel;
-  if (!A.enabled || !finite3(op) || !finite3(np))
-    return collide_point_all(faces, n_faces, op, ov, oF, om, np, nv, c);
+  const bool bounded = A.enabled && finite3(op) && finite3(np);
   float lo[3], hi[3];
   {
     const float o3[3] = {float(op.x), float(op.y), float(op.z)};
@@ -221,48 +245,67 @@ __device__ __forceinline__ bool collide_point(const ObsFace* __restrict__ faces,
       hi[d] = fmaxf(o3[d], n3[d]) + s;
     }
   }
-  for (int k = 0; k < A.n_grids; ++k) {
-    const ObsGrid3& g = A.grids[k];
-    int cb = 0, ce = 0;
-    bool all = false;
-    if (g.n[0] > 0 && hi[0] >= g.lo[0] && lo[0] <= g.hi[0] && hi[1] >= g.lo[1] && lo[1] <= g.hi[1] &&
-        hi[2] >= g.lo[2] && lo[2] <= g.hi[2]) {
-      int idx[3];
-      bool fits = true;
+  const T dtd = T(c.dt_duration);
+  const int n_seg = bounded ? A.n_grids : 1;
+  int hit = -1;
+  T d_old = T(0), d_new = T(0);
+  for (int k = 0; k < n_seg && hit < 0; ++k) {
+    int lb = 0, le = 0;          // linear range of faces
+    int ba = 0, ea = 0, bb = 0, eb = 0;  // cell list [ba, ea) merged with the always list [bb, eb)
+    if (!bounded) {
+      le = n_faces;
+    } else {
+      const ObsGrid3& g = A.grids[k];
+      bool all = false;
+      if (g.n[0] > 0 && hi[0] >= g.lo[0] && lo[0] <= g.hi[0] && hi[1] >= g.lo[1] && lo[1] <= g.hi[1] &&
+          hi[2] >= g.lo[2] && lo[2] <= g.hi[2]) {
+        int idx[3];
+        bool fits = true;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        int i = int(floorf((0.5f * (lo[d] + hi[d]) - g.lo[d]) * g.inv[d]));
-        i = min(max(i, 0), g.n[d] - 1);
-        const float c0 = g.lo[d] + float(i) * g.cell[d] - g.slack;
-        const float c1 = g.lo[d] + float(i + 1) * g.cell[d] + g.slack;
-        fits = fits && lo[d] >= c0 && hi[d] <= c1;
-        idx[d] = i;
-      }
-      if (fits) {
-        const int cell = g.off_base + (idx[0] * g.n[1] + idx[1]) * g.n[2] + idx[2];
-        cb = A.cell_off[cell];
-        ce = A.cell_off[cell + 1];
-      } else {
-        all = true;
-      }
-    }
-    if (all) {  // the box does not fit one cell: test every face of this obstacle in order
-      const T dtd = T(c.dt_duration);
-      for (int f = g.face_base; f < g.face_base + g.n_faces; ++f) {
-        T d_old, d_new;
-        if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
-          collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction),
-                             np, nv);
-          return true;
+        for (int d = 0; d < 3; ++d) {
+          int i = int(floorf((0.5f * (lo[d] + hi[d]) - g.lo[d]) * g.inv[d]));
+          i = min(max(i, 0), g.n[d] - 1);
+          const float c0 = g.lo[d] + float(i) * g.cell[d] - g.slack;
+          const float c1 = g.lo[d] + float(i + 1) * g.cell[d] + g.slack;
+          fits = fits && lo[d] >= c0 && hi[d] <= c1;
+          idx[d] = i;
+        }
+        if (fits) {
+          const int cell = g.off_base + (idx[0] * g.n[1] + idx[1]) * g.n[2] + idx[2];
+          ba = A.cell_off[cell];
+          ea = A.cell_off[cell + 1];
+        } else {
+          all = true;
         }
       }
-      continue;
+      if (all) {  // the box does not fit one cell: every face of this obstacle in order
+        lb = g.face_base;
+        le = g.face_base + g.n_faces;
+      } else {
+        bb = g.always_base;
+        eb = g.always_base + g.n_always;
+      }
     }
-    if (test_faces_from(faces, A.cell_faces, cb, ce, A.always, g.always_base, g.always_base + g.n_always, op, ov, oF,
-                        om, np, nv, c))
-      return true;
+    while (true) {
+      int f;
+      if (lb < le) {
+        f = lb++;
+      } else if (ba < ea || bb < eb) {  // the union of two ascending lists in ascending order
+        const int fa = ba < ea ? A.cell_faces[ba] : 0x7fffffff;
+        const int fb = bb < eb ? A.always[bb] : 0x7fffffff;
+        if (fa <= fb) { f = fa; ++ba; } else { f = fb; ++bb; }
+      } else {
+        break;
+      }
+      if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
+        hit = f;
+        break;
+      }
+    }
   }
-  return false;
+  if (hit < 0) return false;
+  collision_response(faces + hit, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
+  return true;
 }
 
 }  // namespace fgb
