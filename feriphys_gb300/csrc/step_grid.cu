@@ -523,9 +523,17 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothD
     tc::mbar_fence_init();
   }
   int item = blockIdx.x;
+  // persistent mode: thread 0 claims the item after the current one while the
+  // current tile runs (the claims of one CTA only grow, so when the current
+  // item is past the end the claimed one is too, and no item is lost)
+  int next = 0;
+  if (persistent && threadIdx.x == 0) next = atomicAdd(counter, 1);
   while (true) {
     if (persistent) {
-      if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+      if (threadIdx.x == 0) {
+        s_item = next;
+        next = atomicAdd(counter, 1);
+      }
       __syncthreads();  // also: every thread has finished the previous tile
       item = s_item;
       __syncthreads();
