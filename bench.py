@@ -138,9 +138,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def time_cpu_reference(scene_fn, target_s: float, max_steps: int, warmup: int = 1):
+def time_cpu_reference(scene_fn, target_s: float, max_steps: int, warmup: int = 1, keep_points: bool = False):
     """Single-threaded oracle on a bounded sample of the workload: full steps
-    of the same cloth until max_steps or target_s seconds are reached."""
+    of the same cloth until max_steps or target_s seconds are reached.  With
+    keep_points (and no warm-up steps), the oracle's points after the timed
+    steps from the initial state are returned as a second value."""
     import oracle
     from feriphys_gb300 import workloads as W
 
@@ -154,11 +156,32 @@ def time_cpu_reference(scene_fn, target_s: float, max_steps: int, warmup: int = 
         steps += 1
     dt = time.perf_counter() - t0
     n = scene.n_vertices
-    return {"value": n * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d full steps of the %s cloth (%d vertices) on one host core (%s), %.1f s; the "
-                      "reference's step is single-threaded (springy/simulation.rs:28)"
-                      % (steps, scene.name, n, host_cpu()[0], dt),
-            "seconds": dt, "steps": steps}
+    res = {"value": n * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": "%d full steps of the %s cloth (%d vertices) on one host core (%s), %.1f s; the "
+                     "reference's step is single-threaded (springy/simulation.rs:28)"
+                     % (steps, scene.name, n, host_cpu()[0], dt),
+           "seconds": dt, "steps": steps}
+    if keep_points:
+        return res, (mesh.get_points() if warmup <= 0 else None)
+    return res
+
+
+def rel_pos_error(a, b):
+    """max |a - b| / max |b| over the positions of two Stateful point arrays."""
+    a = np.asarray(a, np.float64)[:, 1:4]
+    b = np.asarray(b, np.float64)[:, 1:4]
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def gpu_rollout(mesh, sim, init_points, checkpoints):
+    """Points after each of the (ascending) step counts, from init_points."""
+    mesh.set_points(init_points)
+    out, done = {}, 0
+    for c in checkpoints:
+        sim.step(c - done)
+        done = c
+        out[c] = mesh.get_points()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -618,9 +641,29 @@ def main():
                 "traffic": traffic, "algorithmic_bytes_per_launch": B * n_vert,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
 
+    # error of the timed f32 step against an FP64 rerun of the same step on the GPU and against the
+    # reference's CPU step (the oracle restatement), from the same initial state
+    parity = None
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = time_cpu_reference(lambda: W.c1(n=args.n), args.cpu_seconds, 60, warmup=0)
+    if rank == 0:
+        cps = sorted({c for c in (1, 2, 5, 10, 20, args.rollout) if 1 <= c <= max(1, args.rollout)})
+        p32 = gpu_rollout(mesh, sim, init_points, cps)
+        sim64, mesh64, _ = W.build(scene, fgb)
+        mesh64.set_precision(64)
+        p64 = gpu_rollout(mesh64, sim64, init_points, cps)
+        del sim64, mesh64
+        parity = {"vs_fp64_gpu": {"rel_pos_err_after_steps": {str(c): rel_pos_error(p32[c], p64[c]) for c in cps},
+                                  "how": "the same cloth stepped in f64 on the GPU (general gather path) from the "
+                                         "same initial state, max |x32 - x64| / max |x64| over positions; at this "
+                                         "dt the reference's Euler diverges on this cloth (non-finite at step 62), "
+                                         "which amplifies rounding differences from step ~20 on"}}
+        if world == 1 and not args.no_cpu:
+            cpu, ref_pts = time_cpu_reference(lambda: W.c1(n=args.n), args.cpu_seconds, 60, warmup=0,
+                                              keep_points=True)
+            g_pts = gpu_rollout(mesh, sim, init_points, [cpu["steps"]])[cpu["steps"]]
+            parity["vs_cpu_reference"] = {"steps": cpu["steps"], "rel_pos_err": rel_pos_error(g_pts, ref_pts),
+                                          "kind": "port",
+                                          "how": "the oracle's points after the CPU baseline's timed steps"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -633,7 +676,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
                 "ms_per_step_median": ms_median,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity": parity,
                 "gpu_launches": args.steps * kernels_per_step(mesh, args),
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
                 "device": torch.cuda.get_device_name()}
