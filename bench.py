@@ -266,6 +266,7 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = B * n_vert / (ms * 1e-3) / 1e9
+    parity = batch_fp64_parity(batch, fgb, W, [1, 10, rollout]) if rank == 0 else None
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_roll * rollout,
@@ -280,12 +281,44 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
             "simulated_seconds_per_s": world * dt / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "algorithmic_bytes_per_launch": B * n_vert},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": n_roll * rollout,
+            "cpu_baseline": None, "e2e": None, "gpu_launches": n_roll * rollout, "parity": parity,
             "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite,
             "setup_s": build_s, "device": torch.cuda.get_device_name()}), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def batch_fp64_parity(batch, fgb, W, checkpoints, n_sample=16, seed=12345):
+    """A seeded sample of the batch's cloths advanced as a batch of their own
+    (f32, the batched kernel: each cloth's result equals its result in the
+    full batch) and each alone in f64 on the GPU, from the same initial state;
+    the relative position error per cloth after each checkpoint."""
+    rs = np.random.default_rng(seed)
+    pick = sorted(rs.choice(len(batch.cloths), size=min(n_sample, len(batch.cloths)), replace=False).tolist())
+    sub = W.Batch(batch.name + "-sample", batch.config, [batch.cloths[i] for i in pick], batch.obstacles)
+    s32, m32, _ = W.build_batch(sub, fgb)
+    s64, m64, _ = W.build_batch(sub, fgb)
+    for m in m64:
+        m.set_precision(64)
+    out, done = {}, 0
+    for c in sorted(set(checkpoints)):
+        s32.step(c - done)
+        s64.step(c - done)
+        done = c
+        errs, bad = [], 0
+        for a, b in zip(m32, m64):
+            pa, pb = a.get_points(), b.get_points_f64()
+            if np.isfinite(pa).all() and np.isfinite(pb).all():
+                errs.append(rel_pos_error(pa, pb))
+            else:
+                bad += 1
+        out[str(c)] = {"median": float(np.median(errs)) if errs else None, "max": float(max(errs)) if errs else None,
+                       "nonfinite_cloths": bad}
+    return {"vs_fp64_gpu": {"cloths": len(pick), "rel_pos_err_after_steps": out,
+                            "how": "a seeded sample of the cloths, batched f32 against each stepped alone in f64 on "
+                                   "the GPU; max |x32 - x64| / max |x64| over positions, per cloth; cloths that go "
+                                   "non-finite under the reference's Euler at dt = 1/600 are counted, not compared"}}
 
 
 def rollout_error(p, f):
@@ -399,6 +432,26 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
         done = c
         refs[c] = [m.get_points() for m in pmeshes]
     plain_fine_ms = plain_ms / (ratio * args.coarse_steps)
+    del psim, pmeshes
+
+    # FP64 rerun of the fine solver on the GPU (c3: the cloth; c4: a seeded sample of 16 cloths), the
+    # oracle both the f32 fine solver and the surrogate are measured against below
+    if args.workload == "c3":
+        pick = [0]
+        sim64, meshes64 = build_eval()
+    else:
+        rs = np.random.default_rng(12345)
+        pick = sorted(rs.choice(len(eb.cloths), size=min(16, len(eb.cloths)), replace=False).tolist())
+        sim64, meshes64, _ = W.build_batch(W.Batch(eb.name + "-sample", eb.config, [eb.cloths[i] for i in pick],
+                                                   eb.obstacles), fgb)
+    for m in meshes64:
+        m.set_precision(64)
+    ref64, done = {}, 0
+    for c in checkpoints:
+        sim64.step(ratio * (c - done))
+        done = c
+        ref64[c] = [m.get_points_f64() for m in meshes64]
+    del sim64, meshes64
 
     # surrogate: kernel-only timing (no checks), then the checked rollout
     ssim, smeshes = build_eval()
@@ -420,7 +473,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     kernel_ms = e0.elapsed_time(e1) / k_kernel
     reset()
     chk = fgb.SurrogateCheck.make(energy_growth=args.energy_growth, energy_abs=1e-3, max_strain=args.max_strain)
-    errors, fallbacks, done, sur_ms = {}, 0, 0, 0.0
+    errors, errors64, fallbacks, done, sur_ms = {}, {}, 0, 0, 0.0
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for c in checkpoints:
             e0.record(stream)
@@ -438,6 +491,17 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
             errors[c] = {"mean": float(fin.mean()) if fin.size else None, "max": float(fin.max()) if fin.size else None,
                          "median": float(np.median(fin)) if fin.size else None,
                          "nonfinite_fine": int((~ref_ok).sum()), "nonfinite_surrogate": int((~sur_ok).sum())}
+            e_fine, e_sur = [], []
+            for k, i in enumerate(pick):
+                r64 = ref64[c][k]
+                if not np.isfinite(r64).all():
+                    continue
+                if ref_ok[i]:
+                    e_fine.append(rollout_error(refs[c][i], r64))
+                if sur_ok[i]:
+                    e_sur.append(rollout_error(pts[i], r64))
+            errors64[c] = {"fine_f32": float(np.median(e_fine)) if e_fine else None,
+                           "surrogate": float(np.median(e_sur)) if e_sur else None}
     coarse_ms = sur_ms / args.coarse_steps
     T = ratio * np.float32(dt_f)
     value = world * n_vert * ratio / (coarse_ms * 1e-3)
@@ -456,6 +520,11 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                        "fine_dt": dt_f, "checks": {"energy_growth": args.energy_growth, "max_strain": args.max_strain},
                        "l2": "working set larger than L2 (c4) / one cloth of 1M vertices (c3): not flushed"},
             "error_vs_fine": {str(k): v for k, v in errors.items()},
+            "error_vs_fp64_fine": {"after_coarse_steps": {str(k): v for k, v in errors64.items()},
+                                   "cloths": len(pick),
+                                   "how": "the fine solver rerun in f64 on the GPU from the same initial state; "
+                                          "median over the compared cloths of the same relative RMS position "
+                                          "error as error_vs_fine, for the f32 fine solver and for the surrogate"},
             "fallbacks": fallbacks,
             "simulated_seconds_per_s": {"surrogate": float(T) / (coarse_ms * 1e-3),
                                         "plain_fine": dt_f / (plain_fine_ms * 1e-3),
