@@ -337,7 +337,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     The reference's explicit Euler is unstable at dt = 1/600 s on these cloths
     (the 1024^2 cloth goes non-finite at step 62; at 1/6000 s after ~3,600
     steps, at any position noise), so the fine solver that generates the
-    training data and judges the surrogate runs at --fine-dt (1/30000 s by
+    training data and measures the surrogate runs at --fine-dt (1/30000 s by
     default: finite through the whole evaluation; at 1/6000 s some of the
     uneven cloths also go non-finite within 3000 steps), and one coarse step
     is `ratio` (10) fine steps.
@@ -535,7 +535,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                          "algorithmic_flops_per_launch": SURROGATE_FLOPS_PER_VERTEX * n_vert,
                          "kernel_ms": kernel_ms,
                          "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch; "
-                                 "tensor-pipe utilisation from ncu in profiles/surrogate_step_c3.md"},
+                                 "tensor-pipe utilisation from the committed ncu summary of k_sur_step"},
             "training": {"rows": rows, "collect_and_setup_s": collect_s, "steps": int(args.train_steps),
                          "batch": 65536, "seconds": train_s, "samples_per_s": args.train_steps * 65536 / train_s,
                          "loss_first": float(losses[0]), "loss_last": float(losses[-1])},

@@ -4,8 +4,8 @@
  * C ABI of the drop-in for feriphys's springy-mesh simulation path.  Every
  * entry point mirrors one item of the reference's Rust API (cited as
  * file:line relative to the reference project root); the reference has no FFI
- * of its own, so these are the calls its Rust host would bind (see
- * INTEGRATION.md for the extern "C" block and build.rs).
+ * of its own, so these are the calls its Rust host would bind through an
+ * extern "C" block, with a build.rs that compiles this library.
  *
  * Conventions
  *  - Every function returns 0 (FGB_OK) on success or a negative fgb_status;
@@ -293,7 +293,7 @@ int fgb_sim_destroy(fgb_sim* s);
  * relative velocities), pin flag, relative wind and normal.  Training
  * data comes from the simulation's own fine steps on the GPU; training
  * (forward, backward, Adam) and inference are CUDA kernels of this library.
- * The fine step stays the judge: fgb_sim_step_surrogate checks each cloth's
+ * The fine step stays the reference: fgb_sim_step_surrogate checks each cloth's
  * energy and maximum strain after every coarse step and reverts a failing
  * cloth to `ratio` fine steps.
  *

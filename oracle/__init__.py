@@ -1,7 +1,8 @@
 """The oracle: a CPU restatement of feriphys's cloth step (test infrastructure).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
-this package, and only as the checker (or the timed CPU baseline); the shipped
+this package, and only as the oracle the GPU results are compared with (or the
+timed CPU baseline); the shipped
 library never routes through it.  The C++ restatement lives in
 ``springy_oracle.cpp`` (see its header for the reference file:line map); this
 module builds it with g++ and wraps it with ctypes.

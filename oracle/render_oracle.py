@@ -1,5 +1,5 @@
 """CPU restatement of the reference's render-vertex build -- TEST
-INFRASTRUCTURE ONLY (the checker of fgb_mesh_export_vertices).
+INFRASTRUCTURE ONLY (the oracle of fgb_mesh_export_vertices).
 
 ColoredMesh::from_springy_mesh (graphics/model.rs:72-90) takes
 SpringyMesh::get_vertices (springy_mesh.rs:500-513), computes per-vertex

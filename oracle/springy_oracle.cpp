@@ -1,7 +1,7 @@
 // ORACLE -- test infrastructure only.
 //
 // A CPU restatement of feriphys's spring-mass-damper (cloth) step, used as the
-// checker for the CUDA path in tests/, in __graft_entry__.smoke() and as the
+// oracle of the CUDA path in tests/, in __graft_entry__.smoke() and as the
 // timed CPU baseline in bench.py.  Nothing in the shipped library links it.
 //
 // The reference is a Rust crate that cannot be built here (no cargo/rustc),

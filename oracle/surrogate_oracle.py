@@ -1,6 +1,6 @@
 """CPU restatement of the learned cloth surrogate -- TEST INFRASTRUCTURE ONLY.
 
-Used by tests/ (and nothing else) as the checker of the CUDA surrogate in
+Used by tests/ (and nothing else) as the oracle of the CUDA surrogate in
 feriphys_gb300/csrc/surrogate.cu: the per-vertex input features, the MLP
 54 -> 128 -> 128 -> 3 with the bf16 roundings the tensor-core kernels make,
 its gradient of the mean squared error (the gradient check the training
