@@ -73,6 +73,15 @@ def host_cpu():
     return model, os.cpu_count()
 
 
+def profile_figure(path, key):
+    """A `key: value` line of a committed ncu summary, or None."""
+    try:
+        m = re.search(r"^%s:\s*([0-9.eE+-]+)" % re.escape(key), open(path).read(), re.M)
+    except OSError:
+        return None
+    return float(m.group(1)) if m else None
+
+
 def profile_traffic():
     """DRAM bytes per launch of the step kernel from the committed ncu summary."""
     try:
@@ -164,6 +173,38 @@ def time_cpu_reference(scene_fn, target_s: float, max_steps: int, warmup: int = 
     if keep_points:
         return res, (mesh.get_points() if warmup <= 0 else None)
     return res
+
+
+def time_cpu_batch_sample(batch, target_s: float, steps_per_cloth: int = 10, seed: int = 777):
+    """The oracle on a bounded sample of a batch: seeded random cloths, each
+    in a Simulation of its own (the reference's wind is global per
+    Simulation, springy/config.rs:13), `steps_per_cloth` full steps each,
+    until target_s seconds of stepping."""
+    import oracle
+
+    order = np.random.default_rng(seed).permutation(len(batch.cloths))
+    c = batch.config
+    vsteps, secs, used = 0, 0.0, 0
+    for i in order:
+        args, pins, wind = batch.cloths[int(i)]
+        mesh = oracle.SpringyMesh.cloth(*args, pins)
+        obstacles = [oracle.CollidableMesh(p, q) for p, q in batch.obstacles]
+        sim = oracle.Simulation([mesh], obstacles)
+        sim.set_config(oracle.Config.make(c["integration"], c["dt"], c["gravity"], wind, c["lift_coefficient"],
+                                          c["drag_coefficient"], c["coefficient_of_restitution"],
+                                          c["coefficient_of_friction"]))
+        t0 = time.perf_counter()
+        sim.step(steps_per_cloth)
+        secs += time.perf_counter() - t0
+        vsteps += args[0] * args[1] * steps_per_cloth
+        used += 1
+        if secs >= target_s:
+            break
+    return {"value": vsteps / secs, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d full steps of each of %d seeded random cloths of the batch (%d vertex-steps) on one host "
+                      "core (%s), %.1f s; the reference steps its meshes one after another on one thread "
+                      "(springy/simulation.rs:28)" % (steps_per_cloth, used, vsteps, host_cpu()[0], secs),
+            "seconds": secs}
 
 
 def rel_pos_error(a, b):
@@ -267,6 +308,7 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = B * n_vert / (ms * 1e-3) / 1e9
     parity = batch_fp64_parity(batch, fgb, W, [1, 10, rollout]) if rank == 0 else None
+    cpu = time_cpu_batch_sample(batch, args.cpu_seconds / 2) if rank == 0 and world == 1 and not args.no_cpu else None
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_roll * rollout,
@@ -281,7 +323,7 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
             "simulated_seconds_per_s": world * dt / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "algorithmic_bytes_per_launch": B * n_vert},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": n_roll * rollout, "parity": parity,
+            "cpu_baseline": cpu, "e2e": None, "gpu_launches": n_roll * rollout, "parity": parity,
             "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite,
             "setup_s": build_s, "device": torch.cuda.get_device_name()}), flush=True)
     if dist:
@@ -534,6 +576,8 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                          "frac": achieved / peak, "traffic": None,
                          "algorithmic_flops_per_launch": SURROGATE_FLOPS_PER_VERTEX * n_vert,
                          "kernel_ms": kernel_ms,
+                         "tensor_pipe_active_pct": profile_figure(os.path.join(ROOT, "profiles", "surrogate_step_c3.md"),
+                                                                  "tensor_pipe_active_pct"),
                          "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch; "
                                  "tensor-pipe utilisation from the committed ncu summary of k_sur_step"},
             "training": {"rows": rows, "collect_and_setup_s": collect_s, "steps": int(args.train_steps),
