@@ -319,7 +319,7 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
                                    % (len(meshes), n_vert, S, rollout),
                        "l2": "working set (%.1f GB) larger than L2, not flushed" % (B * n_vert / 1e9),
                        "launch": {"cloths": info[0], "tiles": info[1], "mode": ["per-tile CTAs", "persistent"][info[2]],
-                                  "ctas": info[3]}},
+                                  "ctas": info[3], "tile": "32x%d" % info[4], "chosen_by": "autotuner"}},
             "simulated_seconds_per_s": world * dt / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "algorithmic_bytes_per_launch": B * n_vert},

@@ -162,6 +162,7 @@ def _declare(l):
         "fgb_mesh_set_wind": (I, [P, P]),
         "fgb_sim_set_graphs": (I, [P, I]),
         "fgb_sim_set_batch_mode": (I, [P, I]),
+        "fgb_sim_set_batch_tile": (I, [P, I]),
         "fgb_sim_batch_info": (I, [P, P]),
         "fgb_sim_get_timestep": (I, [P, C.POINTER(C.c_double)]),
         "fgb_sim_synchronize": (I, [P, C.POINTER(C.c_int)]),
@@ -488,12 +489,16 @@ class Simulation:
         """-1 autotuned (default), 0 one CTA per tile, 1 persistent."""
         _check(_lib().fgb_sim_set_batch_mode(self._h, int(mode)))
 
+    def set_batch_tile(self, tile_rows: int):
+        """0 autotuned (default), or batch tiles 32 wide and 4, 8 or 12 rows tall."""
+        _check(_lib().fgb_sim_set_batch_tile(self._h, int(tile_rows)))
+
     def set_graphs(self, enabled: bool):
         _check(_lib().fgb_sim_set_graphs(self._h, 1 if enabled else 0))
 
     def batch_info(self):
-        """(meshes in the batch, work items, launch form, persistent CTAs)."""
-        out = np.zeros(4, np.int64)
+        """(meshes in the batch, work items, launch form, persistent CTAs, tile rows)."""
+        out = np.zeros(5, np.int64)
         _check(_lib().fgb_sim_batch_info(self._h, _ptr(out)))
         return tuple(int(v) for v in out)
 

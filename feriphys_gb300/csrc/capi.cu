@@ -377,6 +377,7 @@ int prepare_batch(fgb_sim* s) {
     }
   }
   const bool membership = grid != s->batch;
+  const bool reshape = s->built_tile_h != s->tile_h;
   std::vector<fgb::ClothDesc> desc(grid.size());
   for (size_t i = 0; i < grid.size(); ++i) {
     fgb_mesh* m = grid[i];
@@ -393,14 +394,15 @@ int prepare_batch(fgb_sim* s) {
     d.cols = int(m->topo.cols);
     for (int k = 0; k < 3; ++k) d.wind[k] = m->has_wind ? m->wind[k] : s->cfg.wind[k];
   }
-  if (membership) {
+  if (membership || reshape) {  // the work list of s->tile_h-row tiles
     std::vector<int> work;
     for (size_t i = 0; i < grid.size(); ++i) {
       int nr, ni;
-      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), nullptr, &nr, &ni);
+      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), s->tile_h, nullptr, &nr, &ni);
       const size_t at = work.size();
       work.resize(at + 4 * size_t(nr + ni));
-      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), work.data() + at, &nr, &ni);
+      fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), s->tile_h, work.data() + at, &nr,
+                       &ni);
     }
     s->n_work = int(work.size() / 4);
     FGB_CUDA(dalloc(s->d_work, work.size() * sizeof(int)));
@@ -408,9 +410,9 @@ int prepare_batch(fgb_sim* s) {
     s->work_host = work;
     if (!s->d_counter) FGB_CUDA(dalloc(s->d_counter, sizeof(int)));
     drop_graphs(s);
-    s->mode = -1;
+    if (membership) s->mode = -1;
   }
-  if (membership || desc.size() != s->desc.size() ||
+  if (membership || reshape || desc.size() != s->desc.size() ||
       std::memcmp(desc.data(), s->desc.data(), desc.size() * sizeof(fgb::ClothDesc)) != 0) {
     if (s->d_desc_cap < desc.size()) {
       FGB_CUDA(dalloc(s->d_desc, desc.size() * sizeof(fgb::ClothDesc)));
@@ -423,7 +425,8 @@ int prepare_batch(fgb_sim* s) {
     std::vector<unsigned char> maps(desc.size() * fgb::kClothMapBytes + 64);
     unsigned char* mp = maps.data() + ((64 - (reinterpret_cast<uintptr_t>(maps.data()) & 63)) & 63);
     bool maps_ok = true;
-    for (size_t i = 0; i < desc.size() && maps_ok; ++i) maps_ok = fgb::encode_cloth_maps(desc[i], mp + i * fgb::kClothMapBytes);
+    for (size_t i = 0; i < desc.size() && maps_ok; ++i)
+      maps_ok = fgb::encode_cloth_maps(desc[i], s->tile_h, mp + i * fgb::kClothMapBytes);
     if (maps_ok) {
       if (s->d_maps_cap < desc.size()) {
         FGB_CUDA(dalloc(s->d_maps, desc.size() * fgb::kClothMapBytes));
@@ -439,6 +442,7 @@ int prepare_batch(fgb_sim* s) {
     FGB_CUDA(cudaStreamSynchronize(bs));
     s->desc = std::move(desc);
   }
+  s->built_tile_h = s->tile_h;
   s->batch = std::move(grid);
   return FGB_OK;
 }
@@ -447,13 +451,16 @@ int batch_launch(fgb_sim* s, int parity, int mode, int ctas) {
   cudaStream_t st = batch_stream(s);
   FGB_CUDA(cudaMemsetAsync(s->d_counter, 0, sizeof(int), st));
   FGB_CUDA(fgb::launch_step_batched(s->d_desc, s->d_work, s->n_work, s->d_counter, parity, mode, ctas,
-                                    make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st, s->d_maps));
+                                    make_consts(s->cfg, s->d_faces, s->n_faces, nullptr, &s->accel), st, s->d_maps,
+                                    nullptr, s->tile_h));
   return FGB_OK;
 }
 
-// Autotuner: times the launch forms on this batch (launches that read the
-// current buffers and write the other ones, so the state is untouched) and
-// caches the winner per GPU and batch size in a text file
+// Autotuner: times every tile height (32 x 4, 32 x 8, 32 x 12 vertex tiles,
+// each with its own block size) and launch form (one CTA per tile, or
+// persistent CTAs at the occupancy the tile allows) on this batch -- launches
+// that read the current buffers and write the other ones, so the state is
+// untouched -- and caches the winner per GPU and batch in a text file
 // ($FGB_AUTOTUNE_CACHE, default ~/.cache/feriphys_gb300/autotune.txt).
 std::string tune_cache_path() {
   if (const char* p = std::getenv("FGB_AUTOTUNE_CACHE")) return p;
@@ -461,75 +468,96 @@ std::string tune_cache_path() {
   return std::string(home ? home : "/tmp") + "/.cache/feriphys_gb300/autotune.txt";
 }
 
-int tune_batch(fgb_sim* s) {
-  if (s->forced_mode >= 0) {
-    s->mode = s->forced_mode;
-    int dev = 0, sms = 0;
-    FGB_CUDA(cudaGetDevice(&dev));
-    FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    s->ctas = fgb::batched_ctas_per_sm() * sms;
-    return FGB_OK;
+int use_launch_form(fgb_sim* s, int tile_h, int mode, int sms) {
+  if (s->tile_h != tile_h) {
+    s->tile_h = tile_h;
+    FGB_CHECK_RC(prepare_batch(s));  // work list and maps for this tile height
   }
+  s->mode = mode;
+  s->ctas = fgb::batched_ctas_per_sm(tile_h) * sms;
+  return FGB_OK;
+}
+
+int tune_batch(fgb_sim* s) {
   int dev = 0;
   FGB_CUDA(cudaGetDevice(&dev));
   cudaDeviceProp prop;
   FGB_CUDA(cudaGetDeviceProperties(&prop, dev));
-  int bucket = 0;
-  while ((1 << bucket) < s->n_work) ++bucket;
+  const int sms = prop.multiProcessorCount;
+  std::vector<int> heights, modes;
+  if (s->forced_tile_h > 0) heights.push_back(s->forced_tile_h);
+  else heights.assign(std::begin(fgb::kBatchTileHeights), std::end(fgb::kBatchTileHeights));
+  if (s->forced_mode >= 0) modes.push_back(s->forced_mode);
+  else modes = {0, 1};
+  if (heights.size() == 1 && modes.size() == 1) return use_launch_form(s, heights[0], modes[0], sms);
+  size_t verts = 0;
+  for (const fgb_mesh* m : s->batch) verts += m->topo.n;
+  int vb = 0, cb = 0;
+  while ((size_t(1) << vb) < verts) ++vb;
+  while ((size_t(1) << cb) < s->batch.size()) ++cb;
   char key[512];
-  std::snprintf(key, sizeof(key), "batched %s sms=%d work=2^%d", prop.name, prop.multiProcessorCount, bucket);
+  std::snprintf(key, sizeof(key), "batched %s sms=%d cloths=2^%d vertices=2^%d heights=%zu modes=%zu", prop.name, sms,
+                cb, vb, heights.size(), modes.size());
   for (char* c = key; *c; ++c)
     if (*c == '\n') *c = ' ';
   const std::string path = tune_cache_path();
   if (FILE* f = std::fopen(path.c_str(), "r")) {
     char line[600];
+    int mode = -1, th = 0;
     while (std::fgets(line, sizeof(line), f)) {
-      int mode = -1, per_sm = 0;
+      int m = -1, t = 0;
       const char* sep = std::strstr(line, " -> ");
       if (!sep || std::string(line, sep - line) != key) continue;
-      if (std::sscanf(sep + 4, "mode=%d ctas_per_sm=%d", &mode, &per_sm) == 2 && (mode == 0 || mode == 1)) {
-        s->mode = mode;
-        s->ctas = per_sm * prop.multiProcessorCount;
+      if (std::sscanf(sep + 4, "mode=%d tile_h=%d", &m, &t) == 2 && (m == 0 || m == 1) &&
+          fgb::batch_tile_height_ok(t) && std::find(heights.begin(), heights.end(), t) != heights.end() &&
+          std::find(modes.begin(), modes.end(), m) != modes.end()) {
+        mode = m;
+        th = t;
       }
     }
     std::fclose(f);
-    if (s->mode >= 0) return FGB_OK;
+    if (mode >= 0) return use_launch_form(s, th, mode, sms);
   }
-  const int per_sm = fgb::batched_ctas_per_sm();
-  const int cand_mode[2] = {0, 1};
   float best = 1e30f;
-  int best_mode = 0;
+  int best_mode = modes[0], best_h = heights[0];
   cudaEvent_t a, b;
   FGB_CUDA(cudaEventCreate(&a));
   FGB_CUDA(cudaEventCreate(&b));
-  for (int ci = 0; ci < 2; ++ci) {
-    const int ctas = per_sm * prop.multiProcessorCount;
-    FGB_CHECK_RC(batch_launch(s, s->parity, cand_mode[ci], ctas));  // warm-up
-    FGB_CUDA(cudaEventRecord(a, batch_stream(s)));
-    for (int r = 0; r < 5; ++r) FGB_CHECK_RC(batch_launch(s, s->parity, cand_mode[ci], ctas));
-    FGB_CUDA(cudaEventRecord(b, batch_stream(s)));
-    FGB_CUDA(cudaEventSynchronize(b));
-    float ms = 0.0f;
-    FGB_CUDA(cudaEventElapsedTime(&ms, a, b));
-    if (ms < best) {
-      best = ms;
-      best_mode = cand_mode[ci];
+  int rc = FGB_OK;
+  for (int th : heights) {
+    for (int mode : modes) {
+      if ((rc = use_launch_form(s, th, mode, sms)) != FGB_OK) break;
+      if ((rc = batch_launch(s, s->parity, mode, s->ctas)) != FGB_OK) break;  // warm-up
+      cudaEventRecord(a, batch_stream(s));
+      for (int r = 0; r < 5 && rc == FGB_OK; ++r) rc = batch_launch(s, s->parity, mode, s->ctas);
+      cudaEventRecord(b, batch_stream(s));
+      float ms = 0.0f;
+      cudaError_t e = cudaEventSynchronize(b);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+      if (rc == FGB_OK && e != cudaSuccess) rc = fail(FGB_ECUDA, cudaGetErrorString(e));
+      if (rc != FGB_OK) break;
+      if (ms < best) {
+        best = ms;
+        best_mode = mode;
+        best_h = th;
+      }
     }
+    if (rc != FGB_OK) break;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  s->mode = best_mode;
-  s->ctas = per_sm * prop.multiProcessorCount;
+  if (rc != FGB_OK) return rc;
+  FGB_CHECK_RC(use_launch_form(s, best_h, best_mode, sms));
   const std::string dir = path.substr(0, path.rfind('/'));
-  std::string cmd_dir = dir;
   // create the cache directory (best effort) and append the result
-  for (size_t i = 1; i <= cmd_dir.size(); ++i)
-    if (i == cmd_dir.size() || cmd_dir[i] == '/') {
-      const std::string sub = cmd_dir.substr(0, i);
+  for (size_t i = 1; i <= dir.size(); ++i)
+    if (i == dir.size() || dir[i] == '/') {
+      const std::string sub = dir.substr(0, i);
       mkdir(sub.c_str(), 0755);
     }
   if (FILE* f = std::fopen(path.c_str(), "a")) {
-    std::fprintf(f, "%s -> mode=%d ctas_per_sm=%d time_ms=%.4f\n", key, best_mode, per_sm, best / 5.0f);
+    std::fprintf(f, "%s -> mode=%d tile_h=%d ctas_per_sm=%d time_ms=%.4f\n", key, best_mode, best_h,
+                 s->ctas / sms, best / 5.0f);
     std::fclose(f);
   }
   return FGB_OK;
@@ -1180,12 +1208,22 @@ int fgb_sim_set_graphs(fgb_sim* s, int enabled) {
   return FGB_OK;
 }
 
-int fgb_sim_batch_info(const fgb_sim* s, int64_t out[4]) {
+int fgb_sim_set_batch_tile(fgb_sim* s, int tile_rows) {
+  if (!s || !(tile_rows == 0 || fgb::batch_tile_height_ok(tile_rows)))
+    return fail(FGB_EINVAL, "tile_rows must be 0 (autotuner), 4, 8 or 12");
+  s->forced_tile_h = tile_rows;
+  s->mode = -1;
+  drop_graphs(s);
+  return FGB_OK;
+}
+
+int fgb_sim_batch_info(const fgb_sim* s, int64_t out[5]) {
   if (!s || !out) return fail(FGB_EINVAL, "null argument");
   out[0] = int64_t(s->batch.size());
   out[1] = s->n_work;
   out[2] = s->mode;
   out[3] = s->ctas;
+  out[4] = s->tile_h;
   return FGB_OK;
 }
 
@@ -1320,7 +1358,8 @@ extern "C" int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream) {
   size_t n_work = 0;
   for (size_t i = 0; i < order.size(); ++i) {
     int nr, ni;
-    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), nullptr, &nr, &ni);
+    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), fgb::kDefaultTileH, nullptr, &nr,
+                     &ni);
     n_work += size_t(nr + ni);
   }
   const size_t desc_off = 256;
@@ -1347,7 +1386,8 @@ extern "C" int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream) {
   std::vector<int> work(4 * n_work);
   for (size_t i = 0, at = 0; i < order.size(); ++i) {
     int nr, ni;
-    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), work.data() + 4 * at, &nr, &ni);
+    fgb::batch_tiles(int(i), int(order[i]->topo.rows), int(order[i]->topo.cols), fgb::kDefaultTileH,
+                     work.data() + 4 * at, &nr, &ni);
     at += size_t(nr + ni);
   }
   for (fgb_mesh* m : order) {  // all cloths read buffer [0] at the first step

@@ -413,13 +413,13 @@ int fine_fallback(fgb_surrogate* g, fgb_sim* s, const std::vector<int>& failing,
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ctas = fgb::batched_ctas_per_sm() * sms;
+    ctas = fgb::batched_ctas_per_sm(s->tile_h) * sms;
   }
   ctas = std::max(1, std::min(ctas, n_fw));
   for (uint32_t j = 0; j < ratio && n_fw > 0; ++j) {
     FGB_CUDA(cudaMemsetAsync(g->d_fcounter, 0, sizeof(int), st));
     FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, g->d_fwork, n_fw, g->d_fcounter, from ^ int(j & 1u), 1, ctas, fc,
-                                      st, s->d_maps));
+                                      st, s->d_maps, nullptr, s->tile_h));
   }
   FGB_CUDA(cudaStreamSynchronize(st));  // the host table must outlive its upload
   return FGB_OK;
@@ -474,7 +474,7 @@ int capture_fallback(fgb_surrogate* g, fgb_sim* s, const Rollout& ro, int par, c
     for (uint32_t j = 0; j < ro.ratio; ++j) {
       FGB_CUDA(cudaMemsetAsync(g->d_fcounter, 0, sizeof(int), bs));
       FGB_CUDA(fgb::launch_step_batched(g->d_fdesc, g->d_fwork, s->n_work, g->d_fcounter, from ^ int(j & 1u), 1,
-                                        ro.ctas, ro.fine, bs, s->d_maps, g->d_counts + 1));
+                                        ro.ctas, ro.fine, bs, s->d_maps, g->d_counts + 1, s->tile_h));
     }
   }
   FGB_CUDA(S::launch_check(g->d_cloths, g->d_tiles, ro.n_tiles, ro.n_cloths, par ^ 1, ro.gforce, g->d_tile_chk,
@@ -592,7 +592,7 @@ int rollout_on_device(fgb_surrogate* g, fgb_sim* s, uint32_t ratio, uint64_t n_c
       int dev = 0, sms = 1;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      ctas = fgb::batched_ctas_per_sm() * sms;
+      ctas = fgb::batched_ctas_per_sm(s->tile_h) * sms;
     }
     ro.ctas = std::max(1, std::min(ctas, s->n_work));
     FGB_CUDA(dgrow(g->d_bidx, g->bidx_cap, bidx.size(), sizeof(int)));

@@ -110,6 +110,9 @@ struct fgb_sim {
   int parity = 0;
   int mode = -1, ctas = 0;                // launch form chosen by the tuner
   int forced_mode = -1;                   // fgb_sim_set_batch_mode (-1: tuner)
+  int tile_h = fgb::kDefaultTileH;        // tile height (rows) chosen by the tuner
+  int forced_tile_h = 0;                  // fgb_sim_set_batch_tile (0: tuner)
+  int built_tile_h = -1;                  // tile height of the uploaded work list and maps
   bool graphs = true;
   std::map<std::pair<uint64_t, int>, cudaGraphExec_t> graph_cache;
   fgb_config graph_cfg;

@@ -58,8 +58,14 @@ struct ClothDesc {
   int skip;  // nonzero: the batched step leaves this cloth untouched (masked fallback steps)
 };
 
+// Batch tiles are 32 wide and kDefaultTileH (or another height the
+// autotuner picks, batch_tile_height_ok) tall.
+constexpr int kDefaultTileH = 8;
+constexpr int kBatchTileHeights[3] = {4, 8, 12};
+bool batch_tile_height_ok(int th);
+
 // Tiles of one cloth for the batch work list: {cloth, tile x, tile y, interior}.
-void batch_tiles(int cloth, int rows, int cols, int* out4 /* may be null */, int* n_ring, int* n_interior);
+void batch_tiles(int cloth, int rows, int cols, int th, int* out4 /* may be null */, int* n_ring, int* n_interior);
 
 // mode 0: one CTA per work item; mode 1: persistent CTAs pulling items from
 // *counter (reset to 0 by the caller before the launch).
@@ -67,16 +73,18 @@ void batch_tiles(int cloth, int rows, int cols, int* out4 /* may be null */, int
 // (encode_cloth_maps) for TMA staging of the tiles.  n_work_dev: null, or the
 // item count in device memory (mode 1 only; n_work is then its upper bound,
 // which sizes the grid).
+// th: the tile height the work list and the maps were made for.
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
                                 int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s,
-                                const void* maps = nullptr, const int* n_work_dev = nullptr);
+                                const void* maps = nullptr, const int* n_work_dev = nullptr,
+                                int th = kDefaultTileH);
 // Sets the launch attributes of the tiled and batched step kernels (done by
 // their launchers on first use; call it before a stream capture).
 cudaError_t prime_step_kernels();
 // Size of one cloth's tensor maps (4 x 128 bytes) and their encoding; false
 // when the driver's encoder is unavailable or an address is misaligned.
 constexpr size_t kClothMapBytes = 4 * 128;
-bool encode_cloth_maps(const ClothDesc& d, void* out /* kClothMapBytes, 64-byte aligned */);
-int batched_ctas_per_sm();
+bool encode_cloth_maps(const ClothDesc& d, int th, void* out /* kClothMapBytes, 64-byte aligned */);
+int batched_ctas_per_sm(int th = kDefaultTileH);
 
 }  // namespace fgb

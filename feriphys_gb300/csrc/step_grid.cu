@@ -157,6 +157,9 @@ struct TileGeom {
   // 2 float4 + 2 float2 = 3 float4
   static constexpr int BUF = (2 * N_TRI > 2 * N_BIND ? (2 * N_TRI > 3 * N_Q ? 2 * N_TRI : 3 * N_Q)
                                                      : (2 * N_BIND > 3 * N_Q ? 2 * N_BIND : 3 * N_Q));
+  // resident CTAs per SM the launch bounds ask for: 64 registers per thread
+  // at TW * TH + 64 threads (32x4: 5, 32x8: 3, 32x12: 2 with 72 registers)
+  static constexpr int MIN_CTAS = TH <= 4 ? 5 : (TH <= 8 ? 3 : 2);
 };
 
 template <int TW, int TH>
@@ -167,6 +170,7 @@ struct Interior {
   static constexpr int NQ = QW * QH;
   // bytes after the staged pos/vel: 5 strut kinds x (float4 (u, s1) + float s2), 3 float4 per quad
   static constexpr int BYTES = 5 * NO * 20 + NQ * 48;
+  static_assert((5 * NO * 20) % 16 == 0, "the quad results must start 16-byte aligned");
 };
 
 // Strut of the compact form: unit vector u and the spring/damper scalars
@@ -473,7 +477,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
 // One launch for all tiles: the boundary ring first (its tiles are slower
 // and then overlap the interior ones instead of running as a lone wave).
 template <int TW, int TH, int HALO, bool TMA>
-__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, int C, TileSplit split, int n_ring,
+__global__ void __launch_bounds__(TW * TH + HALO, TileGeom<TW, TH>::MIN_CTAS) k_step_grid_tiled(int R, int C, TileSplit split, int n_ring,
                                                                       const float4* __restrict__ planes,
                                                                       const float4* __restrict__ pos,
                                                                       const float4* __restrict__ vel,
@@ -508,7 +512,7 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_grid_tiled(int R, in
 // boundary tiles before its interior ones); in persistent mode every CTA
 // pulls items from a global counter until the list is exhausted.
 template <int TW, int TH, int HALO, bool TMA>
-__global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothDesc* __restrict__ cloths,
+__global__ void __launch_bounds__(TW * TH + HALO, TileGeom<TW, TH>::MIN_CTAS) k_step_batched(const ClothDesc* __restrict__ cloths,
                                                                    const int4* __restrict__ work, int n_work,
                                                                    int* __restrict__ counter, int parity,
                                                                    int persistent, StepConsts c,
@@ -562,17 +566,26 @@ __global__ void __launch_bounds__(TW * TH + HALO, 3) k_step_batched(const ClothD
   }
 }
 
-constexpr int kTileW = 32, kTileH = 8, kHalo = 64;
+constexpr int kTileW = 32, kTileH = 8, kHalo = 64;  // the single-cloth kernel's tile; the batch's default
 
-size_t tiled_smem_bytes() {
-  using G = TileGeom<kTileW, kTileH>;
-  using I = Interior<kTileW, kTileH>;
+template <int TH>
+size_t tiled_smem_bytes_t() {
+  using G = TileGeom<kTileW, TH>;
+  using I = Interior<kTileW, TH>;
   return 2 * sizeof(float4) * G::EH * G::EW + size_t(I::BYTES);
 }
 
+size_t tiled_smem_bytes(int th) {
+  switch (th) {
+    case 4: return tiled_smem_bytes_t<4>();
+    case 12: return tiled_smem_bytes_t<12>();
+    default: return tiled_smem_bytes_t<8>();
+  }
+}
+
 // Tensor map of one float4 state array of an R x C grid, seen as R rows of
-// 4C floats, with the tiled kernel's staging box ((TW+4) float4 x (TH+4) rows).
-bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C) {
+// 4C floats, with the staging box of a 32 x th tile ((32+4) float4 x (th+4) rows).
+bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C, int th) {
   using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -591,31 +604,78 @@ bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C) {
   if (!encode || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
   const cuuint64_t dims[2] = {4ull * cuuint64_t(C), cuuint64_t(R)};
   const cuuint64_t strides[1] = {16ull * cuuint64_t(C)};
-  const cuuint32_t box[2] = {4u * (kTileW + 4), kTileH + 4};
+  const cuuint32_t box[2] = {4u * (kTileW + 4), cuuint32_t(th + 4)};
   const cuuint32_t elem[2] = {1, 1};
   return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4*>(base), dims, strides, box, elem,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Ring / interior split of an R x C cloth's 32 x th tiles.  Interior tiles
+// have every neighbour of every vertex inside the cloth:
+// c0 >= 2, c0 + 32 <= C - 2, r0 >= 2, r0 + th <= R - 2.
+TileSplit split_tiles(int rows, int cols, int th) {
+  TileSplit t;
+  t.tx = (cols + kTileW - 1) / kTileW;
+  t.ty = (rows + th - 1) / th;
+  t.bx0 = 1;
+  t.bx1 = cols >= kTileW + 4 ? (cols - 2 - kTileW) / kTileW : 0;
+  t.by0 = 1;
+  t.by1 = rows >= th + 4 ? (rows - 2 - th) / th : 0;
+  return t;
+}
+
+template <int TH>
+cudaError_t prime_batched() {
+  const int smem = int(tiled_smem_bytes_t<TH>());
+  cudaError_t e = cudaFuncSetAttribute(k_step_batched<kTileW, TH, kHalo, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_step_batched<kTileW, TH, kHalo, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  return e;
+}
+
+template <int TH>
+int batched_ctas_per_sm_t() {
+  int n = 0;
+  if (prime_batched<TH>() != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_batched<kTileW, TH, kHalo, true>, kTileW * TH + kHalo,
+                                                    tiled_smem_bytes_t<TH>()) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+template <int TH>
+void launch_batched_t(int grid, const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
+                      int mode, const StepConsts& c, cudaStream_t s, const CUtensorMap* m, const int* n_work_dev) {
+  const size_t smem = tiled_smem_bytes_t<TH>();
+  if (m)
+    k_step_batched<kTileW, TH, kHalo, true><<<grid, kTileW * TH + kHalo, smem, s>>>(
+        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
+  else
+    k_step_batched<kTileW, TH, kHalo, false><<<grid, kTileW * TH + kHalo, smem, s>>>(
+        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
+}
+
 }  // namespace
 
-bool encode_cloth_maps(const ClothDesc& d, void* out) {
+bool batch_tile_height_ok(int th) { return th == 4 || th == 8 || th == 12; }
+
+bool encode_cloth_maps(const ClothDesc& d, int th, void* out) {
   CUtensorMap* m = static_cast<CUtensorMap*>(out);
+  if (!batch_tile_height_ok(th)) return false;
   for (int k = 0; k < 2; ++k)
-    if (!encode_state_map(m + 2 * k, d.pos[k], d.rows, d.cols) || !encode_state_map(m + 2 * k + 1, d.vel[k], d.rows, d.cols))
+    if (!encode_state_map(m + 2 * k, d.pos[k], d.rows, d.cols, th) ||
+        !encode_state_map(m + 2 * k + 1, d.vel[k], d.rows, d.cols, th))
       return false;
   return true;
 }
 
-void batch_tiles(int cloth, int rows, int cols, int* out4, int* n_ring, int* n_interior) {
-  TileSplit t;
-  t.tx = (cols + kTileW - 1) / kTileW;
-  t.ty = (rows + kTileH - 1) / kTileH;
-  t.bx0 = 1;
-  t.bx1 = cols >= kTileW + 4 ? (cols - 2 - kTileW) / kTileW : 0;
-  t.by0 = 1;
-  t.by1 = rows >= kTileH + 4 ? (rows - 2 - kTileH) / kTileH : 0;
+void batch_tiles(int cloth, int rows, int cols, int th, int* out4, int* n_ring, int* n_interior) {
+  const TileSplit t = split_tiles(rows, cols, th);
   const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
   const int ni = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
   const int nr = t.tx * t.ty - ni;
@@ -640,49 +700,42 @@ void batch_tiles(int cloth, int rows, int cols, int* out4, int* n_ring, int* n_i
 cudaError_t prime_step_kernels() {
   static bool done = false;  // per process; the attribute is per function on the current device
   if (done) return cudaSuccess;
-  const int smem = int(tiled_smem_bytes());
+  const int smem = int(tiled_smem_bytes_t<kTileH>());
   cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = prime_batched<4>();
+  if (e == cudaSuccess) e = prime_batched<8>();
+  if (e == cudaSuccess) e = prime_batched<12>();
   done = e == cudaSuccess;
   return e;
 }
 
-int batched_ctas_per_sm() {
-  int n = 0;
-  const size_t smem = tiled_smem_bytes();
-  cudaFuncSetAttribute(k_step_batched<kTileW, kTileH, kHalo, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       int(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_batched<kTileW, kTileH, kHalo, true>,
-                                                    kTileW * kTileH + kHalo, smem) != cudaSuccess)
-    return 1;
-  return n > 0 ? n : 1;
+int batched_ctas_per_sm(int th) {
+  switch (th) {
+    case 4: return batched_ctas_per_sm_t<4>();
+    case 12: return batched_ctas_per_sm_t<12>();
+    default: return batched_ctas_per_sm_t<8>();
+  }
 }
 
 cudaError_t launch_step_batched(const ClothDesc* cloths, const int4* work, int n_work, int* counter, int parity,
                                 int mode, int persistent_ctas, const StepConsts& c, cudaStream_t s, const void* maps,
-                                const int* n_work_dev) {
+                                const int* n_work_dev, int th) {
   if (n_work <= 0) return cudaSuccess;
   if (n_work_dev && mode != 1) return cudaErrorInvalidValue;  // a device count needs the persistent form
-  const size_t smem = tiled_smem_bytes();
+  if (!batch_tile_height_ok(th)) return cudaErrorInvalidValue;
   const cudaError_t ea = prime_step_kernels();
   if (ea != cudaSuccess) return ea;
   const int grid = mode == 1 ? (persistent_ctas < n_work ? persistent_ctas : n_work) : n_work;
   const CUtensorMap* m = static_cast<const CUtensorMap*>(maps);
-  if (m)
-    k_step_batched<kTileW, kTileH, kHalo, true><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
-        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
-  else
-    k_step_batched<kTileW, kTileH, kHalo, false><<<grid, kTileW * kTileH + kHalo, smem, s>>>(
-        cloths, work, n_work, counter, parity, mode == 1, c, m, n_work_dev);
+  switch (th) {
+    case 4: launch_batched_t<4>(grid, cloths, work, n_work, counter, parity, mode, c, s, m, n_work_dev); break;
+    case 12: launch_batched_t<12>(grid, cloths, work, n_work, counter, parity, mode, c, s, m, n_work_dev); break;
+    default: launch_batched_t<8>(grid, cloths, work, n_work, counter, parity, mode, c, s, m, n_work_dev); break;
+  }
   return cudaGetLastError();
 }
 
@@ -694,25 +747,18 @@ cudaError_t launch_step_grid(const GridTopo& g, const float4* pos, const float4*
     k_step_grid_v1<<<(n + 255) / 256, 256, 0, s>>>(g.rows, g.cols, g.params, pos, vel, force_in, pos_out, vel_out,
                                                    c);
   } else {
-    TileSplit t;
-    t.tx = (g.cols + kTileW - 1) / kTileW;
-    t.ty = (g.rows + kTileH - 1) / kTileH;
-    // interior: c0 >= 2, c0 + TW <= C - 2, r0 >= 2, r0 + TH <= R - 2
-    t.bx0 = 1;
-    t.bx1 = g.cols >= kTileW + 4 ? (g.cols - 2 - kTileW) / kTileW : 0;
-    t.by0 = 1;
-    t.by1 = g.rows >= kTileH + 4 ? (g.rows - 2 - kTileH) / kTileH : 0;
+    const TileSplit t = split_tiles(g.rows, g.cols, kTileH);
     const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
     const int n_interior = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
     const int n_ring = t.tx * t.ty - n_interior;
-    const size_t smem = tiled_smem_bytes();
+    const size_t smem = tiled_smem_bytes_t<kTileH>();
     const cudaError_t ea = prime_step_kernels();
     if (ea != cudaSuccess) return ea;
     CUtensorMap map_pos, map_vel;
     std::memset(&map_pos, 0, sizeof(map_pos));
     std::memset(&map_vel, 0, sizeof(map_vel));
-    const bool use_tma =
-        encode_state_map(&map_pos, pos, g.rows, g.cols) && encode_state_map(&map_vel, vel, g.rows, g.cols);
+    const bool use_tma = encode_state_map(&map_pos, pos, g.rows, g.cols, kTileH) &&
+                         encode_state_map(&map_vel, vel, g.rows, g.cols, kTileH);
     if (use_tma)
       k_step_grid_tiled<kTileW, kTileH, kHalo, true><<<n_ring + n_interior, kTileW * kTileH + kHalo, smem, s>>>(
           g.rows, g.cols, t, n_ring, g.params, pos, vel, force_in, pos_out, vel_out, c, map_pos, map_vel);

@@ -235,11 +235,17 @@ int fgb_sim_set_graphs(fgb_sim* s, int enabled);
  * 0 one CTA per tile, 1 persistent CTAs pulling tiles from a work counter. */
 int fgb_sim_set_batch_mode(fgb_sim* s, int mode);
 
+/* Tile of the batched step: 32 vertices wide and tile_rows = 4, 8 or 12
+ * tall (each with its own block size and resident CTAs per SM), or 0
+ * (default) to let the autotuner time all three on the batch.  Extension
+ * with no reference counterpart; results are identical for every tile. */
+int fgb_sim_set_batch_tile(fgb_sim* s, int tile_rows);
+
 /* out[0] meshes in the batch, out[1] work items (tiles), out[2] launch form
  * chosen by the autotuner (0 one CTA per tile, 1 persistent; -1 not yet
- * tuned), out[3] persistent CTAs.  The choice is cached per GPU in
- * $FGB_AUTOTUNE_CACHE (default ~/.cache/feriphys_gb300/autotune.txt). */
-int fgb_sim_batch_info(const fgb_sim* s, int64_t out[4]);
+ * tuned), out[3] persistent CTAs, out[4] tile rows.  The choice is cached
+ * per GPU in $FGB_AUTOTUNE_CACHE (default ~/.cache/feriphys_gb300/autotune.txt). */
+int fgb_sim_batch_info(const fgb_sim* s, int64_t out[5]);
 
 /* Collision search: 1 (default) uses an exact broad phase over the obstacle
  * faces (candidates visited in face order, so the first hit is unchanged);

@@ -192,6 +192,13 @@ def test_extension_entry_points_reject_bad_arguments(fgb):
     assert lib.fgb_mesh_export_indices(null, f, null) == -1
     assert lib.fgb_surrogate_destroy(null) == 0
     assert "null" in lib.fgb_last_error().decode()
+    assert lib.fgb_sim_set_batch_tile(null, 8) == -1
+    sim = fgb.Simulation.new([], [])
+    for bad in (-1, 1, 5, 16):
+        assert lib.fgb_sim_set_batch_tile(sim._h, bad) == -1
+        assert "tile_rows" in lib.fgb_last_error().decode()
+    for ok in (0, 4, 8, 12):
+        assert lib.fgb_sim_set_batch_tile(sim._h, ok) == 0
 
 
 def test_device_build_rejects_bad_input_before_the_gpu(fgb):

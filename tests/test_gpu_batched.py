@@ -57,6 +57,26 @@ def test_batched_equals_alone(fgb, mode, graphs):
     assert got == ref
 
 
+@pytest.mark.parametrize("tile_rows,mode", [(4, 1), (12, 1), (12, 0), (0, -1)])
+def test_every_tile_height_equals_alone(fgb, tile_rows, mode):
+    """32x4, 32x8 and 32x12 tiles (and the autotuner's pick) give every cloth
+    the bits of stepping it alone."""
+    from feriphys_gb300 import workloads as W
+
+    batch = _batch(W)
+    sim, meshes, _ = W.build_batch(batch, fgb)
+    sim.set_batch_tile(tile_rows)
+    sim.set_batch_mode(mode)
+    sim.step(1)
+    sim.step(12)
+    sim.step(7)
+    info = sim.batch_info()
+    assert info[4] == tile_rows if tile_rows else info[4] in (4, 8, 12)
+    ref = _alone(fgb, W, batch, 20)
+    got = [m.get_points().tobytes() for m in meshes]
+    assert got == ref
+
+
 def test_batch_with_general_mesh_and_forces(fgb):
     from feriphys_gb300 import workloads as W
 
