@@ -322,7 +322,9 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
                                   "ctas": info[3], "tile": "32x%d" % info[4], "chosen_by": "autotuner"}},
             "simulated_seconds_per_s": world * dt / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "algorithmic_bytes_per_launch": B * n_vert},
+                         "traffic": profile_figure(os.path.join(ROOT, "profiles", "step_batched_c2.md"),
+                                                   "dram_bytes_per_launch") if args.cloths == 4096 else None,
+                         "algorithmic_bytes_per_launch": B * n_vert},
             "cpu_baseline": cpu, "e2e": None, "gpu_launches": n_roll * rollout, "parity": parity,
             "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite,
             "setup_s": build_s, "device": torch.cuda.get_device_name()}), flush=True)
