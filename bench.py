@@ -780,6 +780,41 @@ def main():
                                           "kind": "port",
                                           "how": "the oracle's points after the CPU baseline's timed steps"}
 
+    # the rows either side of the step: SpringyMesh::new's strut de-duplication on the host and on the
+    # GPU (the same mesh), and the ColoredVertex render export from the device state
+    around = None
+    if rank == 0:
+        t0 = time.perf_counter()
+        m_host = fgb.SpringyMesh.new(scene.positions, scene.indices, scene.mass, 1.0, 1.0)
+        host_s = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m_dev = fgb.SpringyMesh.new(scene.positions, scene.indices, scene.mass, 1.0, 1.0, build_on_device=True)
+        torch.cuda.synchronize()
+        dev_s = time.perf_counter() - t0
+        (kh, ah), (kd, ad) = m_host.get_struts(), m_dev.get_struts()
+        same = bool(np.array_equal(ah, ad) and kh.tobytes() == kd.tobytes())
+        n_tri_struts = len(ah)
+        del m_host, m_dev
+        buf = torch.empty(n_vert * 9, dtype=torch.float32, device="cuda")
+        mesh.export_vertices(buf.data_ptr(), stream_handle=stream.cuda_stream)  # the first call uploads its face lists
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(20):
+            mesh.export_vertices(buf.data_ptr(), stream_handle=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        exp_ms = e0.elapsed_time(e1) / 20
+        around = {"mesh_build": {"host_s": host_s, "device_s": dev_s, "identical": same,
+                                 "how": "SpringyMesh::new of this cloth's positions and triangles (%d struts "
+                                        "de-duplicated from the triangle edges) through fgb_mesh_new and "
+                                        "fgb_mesh_new_device, wall clock" % n_tri_struts},
+                  "render_export": {"ms": exp_ms, "vertices": n_vert, "bytes_written": 36 * n_vert,
+                                    "how": "fgb_mesh_export_vertices: ColoredVertex (position, color, normal "
+                                           "summed over the vertex's faces) into a device buffer, CUDA events"}}
+        del buf
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -791,7 +826,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
                 "ms_per_step_median": ms_median,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity": parity,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity": parity, "around_the_step": around,
                 "gpu_launches": args.steps * kernels_per_step(mesh, args),
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
                 "device": torch.cuda.get_device_name()}
