@@ -305,9 +305,10 @@ __device__ __forceinline__ void epilogue_gelu(uint32_t taddr, const float* __res
 }
 
 // dZ = dH (TMEM) * slope (bf16 tile G), rounded to bf16, written over G.
-__device__ __forceinline__ void epilogue_backward(uint32_t taddr, unsigned char* G, int lt) {
+__device__ __forceinline__ void epilogue_backward(uint32_t taddr, unsigned char* G, int lt, int c0 = 0,
+                                                  int c1 = kHid) {
 #pragma unroll 1
-  for (int cb = 0; cb < kHid; cb += 32) {
+  for (int cb = c0; cb < c1; cb += 32) {
     float d[32];
     tc::tmem_ld32(taddr + cb, d);
 #pragma unroll
@@ -540,11 +541,15 @@ constexpr int kTrG2 = kTrG1 + 32768;       // GELU slopes, then dZ2
 constexpr int kTrDY = kTrG2 + 32768;       // 128 x 16
 constexpr int kTrOnes = kTrDY + 4096;      // 16 x 128 of 1.0
 constexpr int kTrSmem = kTrOnes + 4096;    // 210944 B
+constexpr int kTrThreads = 256;            // two threads per row of a 128-row tile
 
 // tensor-memory columns
 constexpr uint32_t kCA = 0, kCB = 128, kCW2 = 256, kCW1 = 384, kCW3 = 448, kCB2 = 464, kCB1 = 480;
 
-__global__ void __launch_bounds__(128, 1)
+// Two threads per row: thread lt owns row lt % 128 and the hidden columns
+// [64 h, 64 h + 64) with h = lt / 128 in every epilogue; the threads of h = 0
+// form the loss and dY of their row.
+__global__ void __launch_bounds__(kTrThreads, 1)
     k_train(const unsigned char* __restrict__ X, const float* __restrict__ T, int n_tiles,
             const unsigned char* __restrict__ blob, float* __restrict__ partials, float dscale, int* err) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -554,6 +559,7 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ float red[4][4];
   __shared__ float acc[4];  // loss, db3[0..2] of this CTA
   const int lt = threadIdx.x, warp = lt >> 5, lane = lt & 31;
+  const int row = lt & 127, half = lt >> 7, c0 = half * (kHid / 2), c1 = c0 + kHid / 2;
   if (warp == 0) {
     tc::tmem_alloc(&tslot, 512);
     tc::tmem_relinquish();
@@ -567,7 +573,7 @@ __global__ void __launch_bounds__(128, 1)
     fail = 0;
   }
   if (lt < 4) acc[lt] = 0.0f;
-  for (int e = lt; e < 16 * (kHid / 8); e += 128) {  // the ones tile (bf16 1.0 = 0x3F80)
+  for (int e = lt; e < 16 * (kHid / 8); e += kTrThreads) {  // the ones tile (bf16 1.0 = 0x3F80)
     const int r = e / (kHid / 8), kc = e % (kHid / 8);
     *reinterpret_cast<uint4*>(smem + kTrOnes + tc::blk_off(kHid, r, kc * 8)) =
         make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
@@ -579,7 +585,7 @@ __global__ void __launch_bounds__(128, 1)
     tc::bulk_g2s(smem, blob, kBlobBytes, &bar_w);
   }
   bool ok = __syncthreads_and(tc::mbar_wait(&bar_w, 0)) != 0;
-  const uint32_t tmem = tslot, lane_off = uint32_t(warp * 32) << 16;
+  const uint32_t tmem = tslot, lane_off = uint32_t((warp & 3) * 32) << 16;  // the row's TMEM lane quarter
   unsigned char* sX = smem + kTrX;
   unsigned char* sH1 = smem + kTrH1;
   unsigned char* sH2 = smem + kTrH2;
@@ -601,7 +607,7 @@ __global__ void __launch_bounds__(128, 1)
       tc::mbar_arrive_expect_tx(&bar_x, 16384);
       tc::bulk_g2s(sX, X + size_t(t) * 16384, 16384, &bar_x);
     }
-    const float4 tg = reinterpret_cast<const float4*>(T)[size_t(t) * 128 + lt];
+    const float4 tg = reinterpret_cast<const float4*>(T)[size_t(t) * 128 + row];
     if (!(ok = group_wait(&bar_x, ph_x, 0, &fail))) break;
     // layer 1: z1 -> cols [0, 128)
     if (lt == 0) {
@@ -612,7 +618,7 @@ __global__ void __launch_bounds__(128, 1)
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_gelu(tmem + kCA + lane_off, b1, sH1, sG1, lt);
+    epilogue_gelu(tmem + kCA + lane_off, b1, sH1, sG1, row, c0, c1);
     sync_for_mma(0);
     // layer 2: z2 -> cols [128, 256)
     if (lt == 0) {
@@ -623,7 +629,7 @@ __global__ void __launch_bounds__(128, 1)
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_gelu(tmem + kCB + lane_off, b2, sH2, sG2, lt);
+    epilogue_gelu(tmem + kCB + lane_off, b2, sH2, sG2, row, c0, c1);
     sync_for_mma(0);
     // layer 3: y -> cols [0, 16)
     if (lt == 0) {
@@ -634,14 +640,14 @@ __global__ void __launch_bounds__(128, 1)
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    {
+    if (half == 0) {  // warp-uniform
       float y[16];
       tc::tmem_ld16(tmem + kCA + lane_off, y);
       const float r0 = (y[0] + b3[0]) - tg.x, r1 = (y[1] + b3[1]) - tg.y, r2 = (y[2] + b3[2]) - tg.z;
       float ls = (r0 * r0 + r1 * r1) + r2 * r2;
       const uint32_t q0 = pack_bf2(r0 * dscale, r1 * dscale), q1 = pack_bf2(r2 * dscale, 0.0f);
-      *reinterpret_cast<uint4*>(sDY + tc::blk_off(16, lt, 0)) = make_uint4(q0, q1, 0u, 0u);
-      *reinterpret_cast<uint4*>(sDY + tc::blk_off(16, lt, 8)) = make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(sDY + tc::blk_off(16, row, 0)) = make_uint4(q0, q1, 0u, 0u);
+      *reinterpret_cast<uint4*>(sDY + tc::blk_off(16, row, 8)) = make_uint4(0u, 0u, 0u, 0u);
       const float2 e0 = unpack_bf2(q0), e1 = unpack_bf2(q1);
       float s0 = e0.x, s1 = e0.y, s2 = e1.x;
 #pragma unroll
@@ -671,7 +677,7 @@ __global__ void __launch_bounds__(128, 1)
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_backward(tmem + kCB + lane_off, sG2, lt);
+    epilogue_backward(tmem + kCB + lane_off, sG2, row, c0, c1);
     sync_for_mma(0);
     // dW2 (+)= dZ2^T H1; db2 (+)= dZ2^T 1; dH1 = dZ2 W2 -> cols [0, 128)
     if (lt == 0) {
@@ -690,7 +696,7 @@ __global__ void __launch_bounds__(128, 1)
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_backward(tmem + kCA + lane_off, sG1, lt);
+    epilogue_backward(tmem + kCA + lane_off, sG1, row, c0, c1);
     sync_for_mma(0);
     // dW1 (+)= dZ1^T X; db1 (+)= dZ1^T 1
     if (lt == 0) {
@@ -711,26 +717,28 @@ __global__ void __launch_bounds__(128, 1)
   if (ok && !first) {
     float v[32];
 #pragma unroll 1
-    for (int cb = 0; cb < kIn; cb += 32) {
+    for (int cb = half * (kIn / 2); cb < (half + 1) * (kIn / 2); cb += 32) {
       tc::tmem_ld32(tmem + kCW1 + lane_off + cb, v);
-      for (int j = 0; j < 32; ++j) P[kOffW1 + lt * kIn + cb + j] = v[j];
+      for (int j = 0; j < 32; ++j) P[kOffW1 + row * kIn + cb + j] = v[j];
     }
 #pragma unroll 1
-    for (int cb = 0; cb < kHid; cb += 32) {
+    for (int cb = c0; cb < c1; cb += 32) {
       tc::tmem_ld32(tmem + kCW2 + lane_off + cb, v);
-      for (int j = 0; j < 32; ++j) P[kOffW2 + lt * kHid + cb + j] = v[j];
+      for (int j = 0; j < 32; ++j) P[kOffW2 + row * kHid + cb + j] = v[j];
     }
-    float u[16];
-    tc::tmem_ld16(tmem + kCW3 + lane_off, u);
-    for (int o = 0; o < kOutPad; ++o) P[kOffW3 + o * kHid + lt] = o < kOut ? u[o] : 0.0f;
-    tc::tmem_ld16(tmem + kCB1 + lane_off, u);
-    P[kOffB1 + lt] = u[0];
-    tc::tmem_ld16(tmem + kCB2 + lane_off, u);
-    P[kOffB2 + lt] = u[0];
-    if (lt < kOutPad) P[kOffB3 + lt] = (lt < kOut) ? acc[1 + lt] : 0.0f;
-    if (lt == 0) P[kNumParams] = acc[0];
+    if (half == 0) {  // warp-uniform
+      float u[16];
+      tc::tmem_ld16(tmem + kCW3 + lane_off, u);
+      for (int o = 0; o < kOutPad; ++o) P[kOffW3 + o * kHid + row] = o < kOut ? u[o] : 0.0f;
+      tc::tmem_ld16(tmem + kCB1 + lane_off, u);
+      P[kOffB1 + row] = u[0];
+      tc::tmem_ld16(tmem + kCB2 + lane_off, u);
+      P[kOffB2 + row] = u[0];
+      if (lt < kOutPad) P[kOffB3 + lt] = (lt < kOut) ? acc[1 + lt] : 0.0f;
+      if (lt == 0) P[kNumParams] = acc[0];
+    }
   } else {
-    for (int p = lt; p < kPartialStride; p += 128) P[p] = 0.0f;
+    for (int p = lt; p < kPartialStride; p += kTrThreads) P[p] = 0.0f;
   }
   if (!ok && lt == 0) atomicOr(err, 1);
   tc::fence_before_sync();
@@ -1247,7 +1255,7 @@ cudaError_t launch_train(const void* X, const float* T, int n_rows, const void* 
   cudaError_t e = cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
   if (e != cudaSuccess) return e;
   const float dscale = 2.0f / (3.0f * float(n_rows));
-  k_train<<<ctas, 128, kTrSmem, s>>>(static_cast<const unsigned char*>(X), T, n_tiles,
+  k_train<<<ctas, kTrThreads, kTrSmem, s>>>(static_cast<const unsigned char*>(X), T, n_tiles,
                                      static_cast<const unsigned char*>(blob), partials, dscale, err);
   return cudaGetLastError();
 }
