@@ -1,0 +1,29 @@
+"""The C++ mirror of the reference's API (include/feriphys_gb300.hpp) compiles
+against the C ABI and behaves like the reference's types on the host:
+tests/cpp/host_api.cpp, built with g++ and run (no GPU needed)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_cpp_mirror_builds_and_runs(tmp_path):
+    import feriphys_gb300
+
+    lib = feriphys_gb300.library_path()
+    feriphys_gb300._lib()
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    exe = str(tmp_path / "host_api")
+    libdir = os.path.dirname(lib)
+    cmd = [gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "host_api.cpp"), "-o", exe, "-L", libdir, "-lferiphys_gb300",
+           "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
