@@ -9,7 +9,8 @@ Followed line by line (paths relative to the reference project root):
   springy/simulation.rs:27-45   step: accumulate, State, euler_step, update_points, clear
   springy/springy_mesh.rs:515-551, 629-654   forces; 118-172 face normal/area/angles
   springy/springy_mesh.rs:194-196, 223-255   gravity as force, Stateful derivative/as_state
-  state.rs:75-83, utils.rs:5-14               S + S' h, element by element
+  state.rs:75-106, utils.rs:5-21              euler_step S + S' h and the frozen-force
+                                              "rk4_step", element by element
   springy/springy_mesh.rs:423-497             collision response, pin restore
   collidable_mesh.rs:40-47, 107-169           face normal, plane distance, first-hit search
 cgmath 0.18 (the reference's vector library): dot = (x x' + y y') + z z',
@@ -139,12 +140,24 @@ def step(pts, struts, faces, pins, obstacles, cfg):
             F[v] = F[v] + (wk / PI) * (drag + lift)
     for p in pins:
         F[p] = 0.0
-    # State::euler_step: S + S' h with S' = [0, v, F / m, 0, 0, 0]
+    # State::euler_step (S + S' h) or rk4_step, with S' = [0, v, F / m, 0, 0, 0]
     old = pts.copy()
-    deriv = np.zeros_like(pts)
-    deriv[:, 1:4] = V
-    deriv[:, 4:7] = F / pts[:, 0:1]
-    new = pts + deriv * dt
+
+    def deriv(S):
+        d = np.zeros_like(S)
+        d[:, 1:4] = S[:, 4:7]
+        d[:, 4:7] = S[:, 7:10] / S[:, 0:1]
+        return d
+
+    if cfg.get("integration", 0) == 0:
+        new = pts + deriv(pts) * dt
+    else:  # k1..k4 from re-built states; the force is carried, not re-evaluated
+        k1 = deriv(pts)
+        k2 = deriv(pts + k1 * (dt * f(0.5)))
+        k3 = deriv(pts + k2 * (dt * f(0.5)))
+        k4 = deriv(pts + k3 * dt)
+        h6, h3 = dt / f(6.0), dt / f(3.0)
+        new = pts + (((h6 * k1 + h3 * k2) + h3 * k3) + h6 * k4)
     # update_points: first obstacle face crossed, response; then pins restored
     dtd = duration_secs(dt)
     e, mu = f(cfg["restitution"]), f(cfg["friction"])
@@ -177,7 +190,8 @@ def step(pts, struts, faces, pins, obstacles, cfg):
 
 
 @pytest.mark.skipif(_atan2f is None, reason="no libm to take atan2f from")
-def test_second_restatement_matches_the_oracle(orc):
+@pytest.mark.parametrize("integration", [0, 1])
+def test_second_restatement_matches_the_oracle(orc, integration):
     rows, cols, s = 6, 5, f(0.1)
     pins = [rows * cols - cols, rows * cols - 1]
     mesh = orc.SpringyMesh.cloth(rows, cols, float(s), (0.0, 0.0, 0.0), 0.01, 500.0 * s, 0.5 * s, 250.0 * s,
@@ -192,9 +206,9 @@ def test_second_restatement_matches_the_oracle(orc):
     obstacles = [Obstacle(plane_pos[plane_idx[3 * t]], plane_pos[plane_idx[3 * t + 1]], plane_pos[plane_idx[3 * t + 2]])
                  for t in range(2)]
     cfg = dict(gravity=(0.0, -0.0981, 0.0), wind=(2.0, 0.0, 1.0), drag=0.6, lift=0.3, dt=f(1.0 / 1200.0),
-               restitution=0.3, friction=0.2)
+               restitution=0.3, friction=0.2, integration=integration)
     sim = orc.Simulation([mesh], [orc.CollidableMesh(plane_pos, plane_idx)])
-    sim.set_config(orc.Config.make(0, cfg["dt"], cfg["gravity"], cfg["wind"], cfg["lift"], cfg["drag"],
+    sim.set_config(orc.Config.make(integration, cfg["dt"], cfg["gravity"], cfg["wind"], cfg["lift"], cfg["drag"],
                                    cfg["restitution"], cfg["friction"]))
     pts = mesh.get_points()
     hits = 0
