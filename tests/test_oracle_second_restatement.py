@@ -109,7 +109,7 @@ def collided_face(faces, old, new, dtd):
 
 def step(pts, struts, faces, pins, obstacles, cfg):
     """One Simulation::step of one mesh on Stateful points [n, 10] (f32);
-    returns the new points and how many collided."""
+    returns the new points and the obstacle faces hit."""
     pts = pts.copy()
     P, V, F = pts[:, 1:4], pts[:, 4:7], pts[:, 7:10]
     g, wind = np.array(cfg["gravity"], f), np.array(cfg["wind"], f)
@@ -161,13 +161,13 @@ def step(pts, struts, faces, pins, obstacles, cfg):
     # update_points: first obstacle face crossed, response; then pins restored
     dtd = duration_secs(dt)
     e, mu = f(cfg["restitution"]), f(cfg["friction"])
-    hits = 0
+    hits = []
     for i in range(len(new)):
         op, ov, oF, om = old[i, 1:4], old[i, 4:7], old[i, 7:10], old[i, 0]
         face = collided_face(obstacles, op, new[i, 1:4], dtd)
         if face is None:
             continue
-        hits += 1
+        hits.append(face)
         d0, d1 = face.distance(op), face.distance(new[i, 1:4])
         fr = d0 / (d0 - d1)
         cp = op + (dt * fr) * ov
@@ -214,9 +214,54 @@ def test_second_restatement_matches_the_oracle(orc, integration):
     hits = 0
     for k in range(30):
         pts, h = step(pts, struts, faces, pin_list, obstacles, cfg)
-        hits += h
+        hits += len(h)
         sim.step(1)
         ref = mesh.get_points()
         assert pts[:, 1:7].tobytes() == ref[:, 1:7].tobytes(), "step %d: max diff %g" % (
             k, float(np.abs(pts[:, 1:7].astype(np.float64) - ref[:, 1:7]).max()))
     assert hits > 0  # the bottom row reached the plane: the collision response ran too
+
+
+def _plane(axis, at):
+    """Two triangles of the plane {coordinate axis = at} whose normal points
+    along +axis (collidable_mesh.rs face winding)."""
+    if axis == 0:
+        q = [[at, -3, -3], [at, 3, -3], [at, 3, 3], [at, -3, 3]]
+    elif axis == 1:
+        q = [[-3, at, 3], [3, at, 3], [3, at, -3], [-3, at, -3]]
+    else:
+        q = [[-3, -3, at], [3, -3, at], [3, 3, at], [-3, 3, at]]
+    return np.array(q, f), np.array([0, 1, 2, 0, 2, 3], np.uint32)
+
+
+@pytest.mark.skipif(_atan2f is None, reason="no libm to take atan2f from")
+def test_every_projection_axis_of_the_collision_search(orc):
+    """A floor (+y), and walls facing +x and +z that the wind pushes the cloth
+    through: the search drops x, y or z by the reference's signed normal
+    comparisons, and both restatements agree bit for bit."""
+    rows, cols, s = 6, 5, f(0.1)
+    mesh = orc.SpringyMesh.cloth(rows, cols, float(s), (0.0, 0.0, 0.0), 0.01, 500.0 * s, 0.5 * s, 250.0 * s,
+                                 0.5 * s, 50.0 * s, 0.5 * s, [rows * cols - cols])
+    kcl, ab, _ = mesh.get_struts()
+    struts = [((int(a), int(b)), (kcl[j, 0], kcl[j, 1], kcl[j, 2])) for j, (a, b) in enumerate(ab)]
+    faces = [tuple(int(v) for v in fv) for fv in mesh.get_faces()[1]]
+    pin_list = [int(p) for p in mesh.get_pins()]
+    planes = [_plane(1, -0.3005), _plane(0, 0.15002), _plane(2, 0.00002)]
+    obstacles = [Obstacle(pos[idx[3 * t]], pos[idx[3 * t + 1]], pos[idx[3 * t + 2]]) for pos, idx in planes
+                 for t in range(2)]
+    cfg = dict(gravity=(0.0, -0.0981, 0.0), wind=(3.0, 0.0, 3.0), drag=0.6, lift=0.3, dt=f(1.0 / 1200.0),
+               restitution=0.3, friction=0.2)
+    sim = orc.Simulation([mesh], [orc.CollidableMesh(pos, idx) for pos, idx in planes])
+    sim.set_config(orc.Config.make(0, cfg["dt"], cfg["gravity"], cfg["wind"], cfg["lift"], cfg["drag"],
+                                   cfg["restitution"], cfg["friction"]))
+    pts = mesh.get_points()
+    axes = set()
+    for k in range(40):
+        pts, hit = step(pts, struts, faces, pin_list, obstacles, cfg)
+        for face in hit:
+            axes.add(int(np.argmax(np.abs(face.normal()))))
+        sim.step(1)
+        ref = mesh.get_points()
+        assert pts[:, 1:7].tobytes() == ref[:, 1:7].tobytes(), "step %d: max diff %g" % (
+            k, float(np.abs(pts[:, 1:7].astype(np.float64) - ref[:, 1:7]).max()))
+    assert axes == {0, 1, 2}, axes
