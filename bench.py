@@ -225,25 +225,57 @@ def gpu_rollout(mesh, sim, init_points, checkpoints):
     return out
 
 
+def c1_workload(n: int, rollout: int) -> str:
+    """The headline workload's name, identical in both arms (the counts are
+    Cloth::new's: 3(n-1)^2 + 2(n-1) triangle struts, 2(n-2)^2 binding struts,
+    2(n-1)^2 triangles)."""
+    struts = 3 * (n - 1) ** 2 + 2 * (n - 1) + 2 * max(n - 2, 0) ** 2
+    return ("c1 plain cloth %dx%d: %d vertices, %d struts, %d triangles; dt=1/600 Euler; plane + UV sphere "
+            "(32x16); rollouts of %d steps from the initial state" % (n, n, n * n, struts, 2 * (n - 1) ** 2, rollout))
+
+
 def run_reference(args, rank, world):
-    """The reference arm: rank 0 times the CPU implementation; each of the K
-    steps is one full step of the same cloth, capped by --cpu-seconds overall
-    so that any --steps/--warmup finishes within a few minutes."""
+    """The reference arm: rank 0 times the reference's step on the host CPU
+    (the oracle, a single-threaded C++ restatement: the reference itself is
+    Rust and cannot be built here).  W warm-up steps, then exactly K timed
+    steps, each one full step of the same cloth; rollouts restart from the
+    initial state every --rollout steps outside the timed region, as in the
+    GPU arm."""
+    import oracle
     from feriphys_gb300 import workloads as W
 
     if rank != 0:
         return
-    res = time_cpu_reference(lambda: W.c1(n=args.n), args.cpu_seconds, args.steps, warmup=min(args.warmup, 1))
-    value = res["value"]
+    scene = W.c1(n=args.n)
+    sim, mesh, _ = W.build(scene, oracle)
+    init = mesh.get_points()
+    for _ in range(args.warmup):
+        sim.step(1)
+    mesh.set_points(init)
+    secs, since_reset = 0.0, 0
+    for _ in range(args.steps):
+        if since_reset == args.rollout:
+            mesh.set_points(init)
+            since_reset = 0
+        t0 = time.perf_counter()
+        sim.step(1)
+        secs += time.perf_counter() - t0
+        since_reset += 1
+    n = scene.n_vertices
+    value = n * args.steps / secs
+    res = {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": "%d full steps of the %s cloth (%d vertices) on one host core (%s), %.1f s; the reference's "
+                     "step is single-threaded (springy/simulation.rs:28)" % (args.steps, scene.name, n, host_cpu()[0],
+                                                                              secs),
+           "seconds": secs, "steps": args.steps}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * res["seconds"] / res["steps"],
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "c1 plain cloth %dx%d (%d vertices), dt=1/600, Euler, plane+sphere"
-                                   % (args.n, args.n, args.n * args.n), "cpu_threads": 1,
-                       "timed_steps": res["steps"]},
+            "config": {"workload": c1_workload(args.n, args.rollout), "cpu_threads": 1},
             "cpu_baseline": res,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "Rust reference not buildable here (no cargo/rustc); timed: the oracle's C++ restatement"}
+            "note": "Rust reference not buildable here (no cargo/rustc); timed: the oracle's C++ restatement of the "
+                    "reference's step, one thread like the reference"}
     print(json.dumps(line), flush=True)
 
 
@@ -252,7 +284,7 @@ def kernels_per_step(mesh, args):
     return 1
 
 
-def run_batched(args, rank, world, dist, torch, fgb, W):
+def run_batched(args, rank, world, dist, torch, fgb, W, emit=True):
     """4096 uneven cloths advanced together: rollouts of --rollout steps (100
     by default here) captured once as a CUDA graph and replayed; each rollout
     restarts from the initial state outside the timed region.  The working set
@@ -309,8 +341,9 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
     achieved = B * n_vert / (ms * 1e-3) / 1e9
     parity = batch_fp64_parity(batch, fgb, W, [1, 10, rollout]) if rank == 0 else None
     cpu = time_cpu_batch_sample(batch, args.cpu_seconds / 2) if rank == 0 and world == 1 and not args.no_cpu else None
+    line = None
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": n_roll * rollout,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -327,10 +360,11 @@ def run_batched(args, rank, world, dist, torch, fgb, W):
                          "algorithmic_bytes_per_launch": B * n_vert},
             "cpu_baseline": cpu, "e2e": None, "gpu_launches": n_roll * rollout, "parity": parity,
             "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite,
-            "setup_s": build_s, "device": torch.cuda.get_device_name()}), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+            "setup_s": build_s, "device": torch.cuda.get_device_name()}
+        if emit:
+            print(json.dumps(line), flush=True)
+    del sim, meshes
+    return line
 
 
 def batch_fp64_parity(batch, fgb, W, checkpoints, n_sample=16, seed=12345):
@@ -375,7 +409,7 @@ SURROGATE_FLOPS_PER_VERTEX = 2 * (54 * 128 + 128 * 128 + 128 * 3)  # 47,360 algo
 SURROGATE_MMA_FLOPS_PER_VERTEX = 2 * (64 * 128 + 128 * 128 + 128 * 16)  # as issued (padded K and N)
 
 
-def run_surrogate(args, rank, world, dist, torch, fgb, W):
+def run_surrogate(args, rank, world, dist, torch, fgb, W, emit=True):
     """c3: the learned surrogate on the 1024^2 cloth; c4: on 4096 uneven cloths.
 
     The reference's explicit Euler is unstable at dt = 1/600 s on these cloths
@@ -461,8 +495,8 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     psim.set_stream(stream.cuda_stream)
     psim.step(0)
     n_vert = sum(m.n_points for m in pmeshes)
-    checkpoints = sorted({c for c in (1, 10, 100, args.coarse_steps) if c <= args.coarse_steps})
-    refs = {}
+    checkpoints = sorted({c for c in (1, 10, 100, 300, args.coarse_steps) if c <= args.coarse_steps})
+    refs, plain_cum = {}, {}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     done = 0
@@ -473,6 +507,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
         e1.record(stream)
         torch.cuda.synchronize()
         plain_ms += e0.elapsed_time(e1)
+        plain_cum[c] = plain_ms
         done = c
         refs[c] = [m.get_points() for m in pmeshes]
     plain_fine_ms = plain_ms / (ratio * args.coarse_steps)
@@ -518,6 +553,8 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
     reset()
     chk = fgb.SurrogateCheck.make(energy_growth=args.energy_growth, energy_abs=1e-3, max_strain=args.max_strain)
     errors, errors64, fallbacks, done, sur_ms = {}, {}, 0, 0, 0.0
+    n_cloths_eval = len(smeshes)
+    horizon = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for c in checkpoints:
             e0.record(stream)
@@ -526,6 +563,9 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
             torch.cuda.synchronize()
             sur_ms += e0.elapsed_time(e1)
             done = c
+            # over the first c coarse steps: the same simulated time c*T in both solvers
+            horizon[c] = {"speedup_vs_plain": plain_cum[c] / sur_ms,
+                          "fallback_fraction": fallbacks / float(n_cloths_eval * c)}
             pts = [m.get_points() for m in smeshes]
             ref_ok = np.array([np.isfinite(f).all() for f in refs[c]])
             sur_ok = np.array([np.isfinite(p).all() for p in pts])
@@ -546,6 +586,8 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                     e_sur.append(rollout_error(pts[i], r64))
             errors64[c] = {"fine_f32": float(np.median(e_fine)) if e_fine else None,
                            "surrogate": float(np.median(e_sur)) if e_sur else None}
+            horizon[c]["median_rel_pos_err"] = errors[c]["median"]
+            horizon[c]["max_rel_pos_err"] = errors[c]["max"]
     coarse_ms = sur_ms / args.coarse_steps
     T = ratio * np.float32(dt_f)
     value = world * n_vert * ratio / (coarse_ms * 1e-3)
@@ -554,8 +596,9 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     peak = peaks["bf16_tflops"] if peaks else 1900.0
     achieved = SURROGATE_FLOPS_PER_VERTEX * n_vert / (kernel_ms * 1e-3) / 1e12
+    line = None
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": "cloth vertex-steps/s (fine-step equivalents) with the learned surrogate", "value": value,
             "unit": UNIT, "n_gpus": world, "steps": args.coarse_steps, "warmup": 5,
             "ms_per_step": coarse_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -570,6 +613,11 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                                           "median over the compared cloths of the same relative RMS position "
                                           "error as error_vs_fine, for the f32 fine solver and for the surrogate"},
             "fallbacks": fallbacks,
+            "fallback_fraction": fallbacks / float(n_cloths_eval * args.coarse_steps),
+            "by_horizon": {str(k): v for k, v in horizon.items()},
+            "target": "north star: >= 5x the simulated seconds per second of the plain solver at <= 1e-2 relative "
+                      "position error after 1000 coarse steps; by_horizon gives the speed-up over the first c "
+                      "coarse steps and the error after them",
             "simulated_seconds_per_s": {"surrogate": float(T) / (coarse_ms * 1e-3),
                                         "plain_fine": dt_f / (plain_fine_ms * 1e-3),
                                         "ratio": (float(T) / coarse_ms) / (dt_f / plain_fine_ms)},
@@ -578,18 +626,23 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W):
                          "frac": achieved / peak, "traffic": None,
                          "algorithmic_flops_per_launch": SURROGATE_FLOPS_PER_VERTEX * n_vert,
                          "kernel_ms": kernel_ms,
+                         "mma_issued_tflops": SURROGATE_MMA_FLOPS_PER_VERTEX * n_vert / (kernel_ms * 1e-3) / 1e12,
                          "tensor_pipe_active_pct": profile_figure(os.path.join(ROOT, "profiles", "surrogate_step_c3.md"),
                                                                   "tensor_pipe_active_pct"),
                          "note": "k_sur_step: features + 3 MMA layers + GELU epilogues + integration in one launch; "
-                                 "tensor-pipe utilisation from the committed ncu summary of k_sur_step"},
+                                 "achieved and mma_issued_tflops measured in this run (CUDA events, the padded "
+                                 "K = 64 / N = 16 MMA shapes for the latter); tensor_pipe_active_pct is "
+                                 "sm__pipe_tensor_cycles_active from the committed ncu summary "
+                                 "profiles/surrogate_step_c3.md"},
             "training": {"rows": rows, "collect_and_setup_s": collect_s, "steps": int(args.train_steps),
                          "batch": 65536, "seconds": train_s, "samples_per_s": args.train_steps * 65536 / train_s,
                          "loss_first": float(losses[0]), "loss_last": float(losses[-1])},
             "cpu_baseline": None, "e2e": None, "gpu_launches": None,
-            "clocks": clk.summary(), "device": torch.cuda.get_device_name()}), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
+            "clocks": clk.summary(), "device": torch.cuda.get_device_name()}
+        if emit:
+            print(json.dumps(line), flush=True)
+    del ssim, smeshes, sur
+    return line
 
 
 def main():
@@ -603,6 +656,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="c1 only: leave out the batched (c2) and batched-surrogate (c4) results of the line")
     ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general gather, 2 tiled grid, 3 untiled grid")
     ap.add_argument("--probe", action="store_true", help="report the first step whose state is non-finite")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
@@ -650,10 +705,12 @@ def main():
     import feriphys_gb300 as fgb
     from feriphys_gb300 import workloads as W
 
-    if args.workload == "c2":
-        return run_batched(args, rank, world, dist, torch, fgb, W)
-    if args.workload in ("c3", "c4"):
-        return run_surrogate(args, rank, world, dist, torch, fgb, W)
+    if args.workload in ("c2", "c3", "c4"):
+        (run_batched if args.workload == "c2" else run_surrogate)(args, rank, world, dist, torch, fgb, W)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
 
     scene = W.c1(n=args.n, seed=rank)
     sim, mesh, _ = W.build(scene, fgb)
@@ -746,6 +803,37 @@ def main():
            "d2h_bytes_per_step": 40 * n_vert, "ms_per_step": 1e3 * e2e_s,
            "path": "fgb_mesh_set_points + fgb_sim_step + fgb_mesh_get_points, pinned host buffers"}
 
+    # end to end in the shape of the reference's render loop (demos/cloth.rs:107-138): the state stays on
+    # the GPU, every step is followed by a read of the positions only (12 B per vertex) into pinned memory;
+    # rollouts restart from the initial state every --rollout steps outside the timed region
+    pos_pinned = torch.empty((n_vert, 3), dtype=torch.float32, pin_memory=True)
+    pos_host = pos_pinned.numpy()
+    mesh.set_points(init_points)
+    for _ in range(3):
+        sim.step(1)
+        mesh.get_positions(out=pos_host)
+    mesh.set_points(init_points)
+    pos_s, since = 0.0, 0
+    for i in range(args.e2e_steps):
+        if since == args.rollout:
+            mesh.set_points(init_points)
+            since = 0
+        t0 = time.perf_counter()
+        sim.step(1)
+        mesh.get_positions(out=pos_host)
+        pos_s += time.perf_counter() - t0
+        since += 1
+    pos_s /= args.e2e_steps
+    if dist:
+        t = torch.tensor([pos_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        pos_s = float(t.item())
+    e2e_positions = {"value": world * n_vert / pos_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                     "d2h_bytes_per_step": 12 * n_vert, "ms_per_step": 1e3 * pos_s,
+                     "path": "fgb_sim_step + fgb_mesh_get_positions into a pinned host buffer (state resident on "
+                             "the GPU, positions read back every step, as a render loop does)"}
+    del pos_pinned, pos_host
+
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else None
     peak = peaks["hbm_gbs"] if peaks else 6800.0
@@ -819,17 +907,35 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-                "config": {"workload": "c1 plain cloth %dx%d: %d vertices, %d struts, %d triangles; dt=1/600 "
-                                       "Euler; plane + UV sphere (32x16); rollouts of %d steps from the "
-                                       "initial state" % (args.n, args.n, n_vert, n_struts, n_faces, args.rollout),
+                "config": {"workload": c1_workload(args.n, args.rollout),
                            "l2": "flushed (256 MB write) before every timed step",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
                 "ms_per_step_median": ms_median,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "parity": parity, "around_the_step": around,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_positions": e2e_positions,
+                "parity": parity, "around_the_step": around,
                 "gpu_launches": args.steps * kernels_per_step(mesh, args),
                 "clocks": clk.summary(), "wall_s_timed": wall, "nonfinite_rollouts": nonfinite_steps,
                 "device": torch.cuda.get_device_name()}
+    # the other half of the metric: the uneven-cloth batch, plain and with the learned surrogate
+    # (each its own timed region, after the headline's)
+    extras = [] if args.no_extras else ["batched", "surrogate"]
+    if extras:
+        del sim, mesh, flush
+        torch.cuda.synchronize()
+        sub = argparse.Namespace(**vars(args))
+        sub.rollout = 100
+        sub.steps = max(args.steps, 100)
+        sub.workload = "c2"
+        b = run_batched(sub, rank, world, dist, torch, fgb, W, emit=False)
+        torch.cuda.synchronize()
+        sub = argparse.Namespace(**vars(args))
+        sub.workload = "c4"
+        su = run_surrogate(sub, rank, world, dist, torch, fgb, W, emit=False)
+        if rank == 0:
+            line["batched"] = b
+            line["surrogate"] = su
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

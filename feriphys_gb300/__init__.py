@@ -318,8 +318,10 @@ class SpringyMesh:
             raise ValueError("expected %d floats" % (10 * self.n_points))
         _check(_lib().fgb_mesh_set_points(self._h, _ptr(pts)))
 
-    def get_positions(self) -> np.ndarray:
-        out = np.empty((self.n_points, 3), np.float32)
+    def get_positions(self, out=None) -> np.ndarray:
+        """Positions as [n, 3] float32 (a pinned ``out`` is written by the GPU directly)."""
+        if out is None:
+            out = np.empty((self.n_points, 3), np.float32)
         _check(_lib().fgb_mesh_get_positions(self._h, _ptr(out)))
         return out
 

@@ -19,6 +19,7 @@
 
 #include "feriphys_gb300.h"
 #include "handles.h"
+#include "per_device.h"
 #include "kernels.h"
 #include "mesh_build.h"
 #include "obstacle_accel.h"
@@ -913,6 +914,15 @@ int fgb_mesh_get_positions(fgb_mesh* m, float* out) {
     return FGB_OK;
   }
   FGB_CUDA(cudaSetDevice(m->device));
+  if (float* direct = mapped_host(out)) {
+    // pinned host rows: the kernel writes them across the host link itself
+    if (m->precision == 64)
+      FGB_CUDA(fgb::launch_positions<double>(int(n), m->pos[m->cur], direct, m->stream));
+    else
+      FGB_CUDA(fgb::launch_positions<float>(int(n), m->pos[m->cur], direct, m->stream));
+    FGB_CUDA(cudaStreamSynchronize(m->stream));
+    return FGB_OK;
+  }
   FGB_CHECK_RC(ensure_io(m, 3 * sizeof(float) * n));
   if (m->precision == 64)
     FGB_CUDA(fgb::launch_positions<double>(int(n), m->pos[m->cur], m->d_io, m->stream));
@@ -1145,6 +1155,13 @@ int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const*
   FGB_CHECK_RC(make_obstacle_faces(obstacles, n_obstacles, faces));
   for (uint64_t i = 0; i < n_meshes; ++i)
     if (!meshes[i]) return fail(FGB_EINVAL, "null mesh");
+  // one simulation steps its meshes with one kernel per step on one device:
+  // meshes created on different devices cannot share it
+  for (uint64_t i = 1; i < n_meshes; ++i)
+    if (meshes[i]->device != meshes[0]->device)
+      return fail(FGB_EINVAL, "meshes of one simulation must be on one device (mesh " + std::to_string(i) +
+                                  " is on device " + std::to_string(meshes[i]->device) + ", mesh 0 on device " +
+                                  std::to_string(meshes[0]->device) + ")");
   fgb_sim* s = new (std::nothrow) fgb_sim();
   if (!s) return fail(FGB_ENOMEM, "out of host memory");
   s->meshes.assign(meshes, meshes + n_meshes);
@@ -1378,6 +1395,7 @@ extern "C" int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream) {
       return fail(FGB_ESTATE, "mesh not prepared: call fgb_sim_step(sim, 0) once during set-up (and after any "
                               "topology, pin or precision change)");
   }
+  const fgb::DeviceGuard keep_device;  // the caller's current device is restored on every return
   FGB_CUDA(cudaSetDevice(s->meshes[0]->device));
   unsigned char* scratch = nullptr;
   FGB_CHECK_RC(static_scratch(&scratch));
@@ -1445,7 +1463,8 @@ extern "C" int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream) {
     m->has_force = m->has_force && n_steps == 0;
     m->staged = false;
   }
-  // the batched path's own parity no longer matches these meshes
-  s->batch.clear();
+  // The regular batched step keeps its work list, launch form and graphs: its
+  // next call finds m->cur != s->parity where the buffers were swapped,
+  // swaps them back and re-uploads the cloth table (prepare_batch).
   return FGB_OK;
 }

@@ -40,14 +40,29 @@ __global__ void k_pack(int n, const Vec4<T>* __restrict__ pos, const Vec4<T>* __
   }
 }
 
+// Positions as 3 f32 per vertex.  A block's 256 rows (3 KB) are assembled in
+// shared memory and leave as 16-byte chunks when the destination allows it,
+// so a pinned host buffer written across the host link gets whole lines.
 template <class T>
-__global__ void k_positions(int n, const Vec4<T>* __restrict__ pos, float* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Vec4<T> P = pos[i];
-  out[3 * size_t(i)] = float(P.x);
-  out[3 * size_t(i) + 1] = float(P.y);
-  out[3 * size_t(i) + 2] = float(P.z);
+__global__ void __launch_bounds__(256) k_positions(int n, const Vec4<T>* __restrict__ pos, float* __restrict__ out) {
+  __shared__ __align__(16) float s[3 * 256];
+  const int base = blockIdx.x * 256;
+  const int i = base + threadIdx.x;
+  if (i < n) {
+    const Vec4<T> P = pos[i];
+    s[3 * threadIdx.x] = float(P.x);
+    s[3 * threadIdx.x + 1] = float(P.y);
+    s[3 * threadIdx.x + 2] = float(P.z);
+  }
+  __syncthreads();
+  const int rows = min(256, n - base);
+  float* dst = out + 3 * size_t(base);
+  if (rows == 256 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    if (threadIdx.x < 192)
+      reinterpret_cast<float4*>(dst)[threadIdx.x] = reinterpret_cast<const float4*>(s)[threadIdx.x];
+  } else {
+    for (int k = threadIdx.x; k < 3 * rows; k += 256) dst[k] = s[k];
+  }
 }
 
 template <class T>

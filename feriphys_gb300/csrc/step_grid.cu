@@ -9,10 +9,12 @@
 #include <cuda.h>
 
 #include <cstring>
+#include <mutex>
 
 #include "fastdiv.cuh"
 #include "grid_order.h"
 #include "kernels.h"
+#include "per_device.h"
 #include "physics.cuh"
 #include "tc05.cuh"
 
@@ -590,9 +592,8 @@ bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C, int th) 
                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
   static Encode encode = nullptr;
-  static bool looked_up = false;
-  if (!looked_up) {
-    looked_up = true;
+  static std::once_flag looked_up;  // the driver entry point is process-wide
+  std::call_once(looked_up, [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
@@ -600,7 +601,7 @@ bool encode_state_map(CUtensorMap* m, const float4* base, int R, int C, int th) 
       encode = reinterpret_cast<Encode>(fn);
     else
       cudaGetLastError();
-  }
+  });
   if (!encode || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
   const cuuint64_t dims[2] = {4ull * cuuint64_t(C), cuuint64_t(R)};
   const cuuint64_t strides[1] = {16ull * cuuint64_t(C)};
@@ -698,19 +699,20 @@ void batch_tiles(int cloth, int rows, int cols, int th, int* out4, int* n_ring, 
 }
 
 cudaError_t prime_step_kernels() {
-  static bool done = false;  // per process; the attribute is per function on the current device
-  if (done) return cudaSuccess;
-  const int smem = int(tiled_smem_bytes_t<kTileH>());
-  cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) e = prime_batched<4>();
-  if (e == cudaSuccess) e = prime_batched<8>();
-  if (e == cudaSuccess) e = prime_batched<12>();
-  done = e == cudaSuccess;
-  return e;
+  // the attribute is per function and per device: set once on each device used
+  static PerDeviceOnce once;
+  return once.run([] {
+    const int smem = int(tiled_smem_bytes_t<kTileH>());
+    cudaError_t e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_step_grid_tiled<kTileW, kTileH, kHalo, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = prime_batched<4>();
+    if (e == cudaSuccess) e = prime_batched<8>();
+    if (e == cudaSuccess) e = prime_batched<12>();
+    return e;
+  });
 }
 
 int batched_ctas_per_sm(int th) {

@@ -20,6 +20,7 @@
 
 #include "devmath.cuh"
 #include "grid_order.h"
+#include "per_device.h"
 #include "physics.cuh"
 #include "surrogate.h"
 #include "tc05.cuh"
@@ -1164,26 +1165,22 @@ __global__ void k_accept(const float2* __restrict__ cloth_out, int n_cloths, con
   if (c < n_cloths && fail[c]) e_old[c] = cloth_out[c].x;
 }
 
-int g_sms = 0;
-
+// SMs of the current device (asked every time: a process may use several devices).
 int sm_count() {
-  if (g_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sms <= 0) g_sms = 1;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
   }
-  return g_sms;
+  return sms > 0 ? sms : 1;
 }
 
 template <int G, int H>
 cudaError_t sur_step_attr() {
-  static bool done = false;  // per process; the attribute is per function on the current device
-  if (done) return cudaSuccess;
-  const cudaError_t e =
-      cudaFuncSetAttribute(k_sur_step<G, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBlobSmem + G * 32768);
-  done = e == cudaSuccess;
-  return e;
+  // the attribute is per function and per device: set once on each device used
+  static PerDeviceOnce once;
+  return once.run(
+      [] { return cudaFuncSetAttribute(k_sur_step<G, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBlobSmem + G * 32768); });
 }
 
 template <int G, int H>

@@ -204,7 +204,9 @@ int fgb_collidable_destroy(fgb_obstacle* o);
 /* Simulation::new -- springy/simulation.rs:17-25 (starts from
  * Config::default()).  The simulation borrows the meshes and obstacles:
  * step it only while they live.  fgb_sim_destroy never touches them, so the
- * handles may be destroyed in any order. */
+ * handles may be destroyed in any order.  Every mesh must have been created
+ * with the same CUDA device current (a mesh belongs to the device current at
+ * its creation); meshes of different devices give FGB_EINVAL. */
 int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
                 fgb_sim** out);
 
@@ -276,7 +278,10 @@ int fgb_sim_set_stream(fgb_sim* s, void* stream);
  * array's device address, so make that first call before any stream capture.
  * Every call reuses the same array: calls that overlap on the GPU (other
  * streams or threads) race.  stream: a cudaStream_t, or NULL for the
- * simulation's own stream; the call returns when the steps have finished. */
+ * simulation's own stream; the call returns when the steps have finished.
+ * The calling thread's current device is the same on return as on entry, and
+ * regular fgb_sim_step calls on the same simulation may come before or after
+ * it. */
 int fgb_sim_step_static(fgb_sim* s, uint64_t n_steps, void* stream);
 
 /* Simulation::get_timestep -- springy/simulation.rs:47-49, as

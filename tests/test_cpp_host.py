@@ -27,3 +27,29 @@ def test_cpp_mirror_builds_and_runs(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+def test_sim_rejects_meshes_of_different_devices(tmp_path):
+    """fgb_sim_new refuses meshes created on different devices (white-box:
+    tests/cpp/sim_devices.cpp marks a mesh's device through the internal
+    handle layout; no GPU, no launch)."""
+    import feriphys_gb300
+
+    lib = feriphys_gb300.library_path()
+    feriphys_gb300._lib()
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    from feriphys_gb300 import build as fbuild
+
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(fbuild._nvcc())), "include")
+    exe = str(tmp_path / "sim_devices")
+    libdir = os.path.dirname(lib)
+    cmd = [gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-I",
+           os.path.join(ROOT, "feriphys_gb300", "csrc"), "-I", cuda_inc,
+           os.path.join(ROOT, "tests", "cpp", "sim_devices.cpp"), "-o", exe, "-L", libdir, "-lferiphys_gb300",
+           "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
