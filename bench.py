@@ -463,14 +463,36 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W, emit=True):
                                                                                     train_side))
     else:
         tb = W.c2(n_cloths=args.train_cloths * 64, seed=1000, dt=dt_f)
-        tsim, _, _ = W.build_batch(tb, fgb)
+        tsim, tmeshes, _ = W.build_batch(tb, fgb)
         ring = args.ring
         sur.reserve(ring)
         per = max(1, ring // tb.n_vertices)
-        for _ in range(per):
-            sur.collect(tsim, ratio, 1)
-            tsim.step(ratio * args.collect_skip)
-        del tsim
+        noise_rng = np.random.default_rng(4242)
+        perturb = args.train_noise_p > 0 or args.train_noise_v > 0
+        for snap in range(per):
+            if perturb and snap % 2 == 1:
+                # every other snapshot is taken from a perturbed copy of the state (free vertices: positions
+                # + N(0, noise_p h), velocities + N(0, noise_v h / T)), so the network also learns the
+                # dynamics just off the trajectory, where its own steps drift; the clean state is then
+                # restored and the trajectory continues from it
+                saved = [m.get_points() for m in tmeshes]
+                for m, pts, (cargs, pins, _) in zip(tmeshes, saved, tb.cloths):
+                    h = cargs[2]
+                    q = pts.copy()
+                    free = np.ones(len(q), bool)
+                    free[np.asarray(pins, np.int64)] = False
+                    q[free, 1:4] += noise_rng.normal(0.0, args.train_noise_p * h, (int(free.sum()), 3))
+                    q[free, 4:7] += noise_rng.normal(0.0, args.train_noise_v * h / (ratio * dt_f),
+                                                     (int(free.sum()), 3))
+                    m.set_points(q)
+                sur.collect(tsim, ratio, 1)
+                for m, pts in zip(tmeshes, saved):
+                    m.set_points(pts)
+                tsim.step(ratio * (args.collect_skip + 1))
+            else:
+                sur.collect(tsim, ratio, 1)
+                tsim.step(ratio * args.collect_skip)
+        del tsim, tmeshes
         eb = W.c2(n_cloths=args.cloths, seed=rank, dt=dt_f)
 
         def build_eval():
@@ -674,6 +696,10 @@ def main():
     ap.add_argument("--collect-skip", type=int, default=0,
                     help="coarse steps between collected snapshots (0: c3 60; c4 coarse-steps/20, so that the "
                          "snapshots span the evaluated horizon)")
+    ap.add_argument("--train-noise-p", type=float, default=0.0,
+                    help="c4: position noise (fraction of the rest spacing) of every other training snapshot")
+    ap.add_argument("--train-noise-v", type=float, default=0.0,
+                    help="c4: velocity noise (fraction of spacing per coarse step) of every other training snapshot")
     ap.add_argument("--energy-growth", type=float, default=0.05)
     ap.add_argument("--max-strain", type=float, default=1000.0)
     args = ap.parse_args()

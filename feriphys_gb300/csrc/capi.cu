@@ -299,6 +299,7 @@ fgb::StepConsts make_consts(const fgb_config& cfg, const fgb::ObsFace* faces, in
   c.neg_lift = -1.0f * cfg.lift_coefficient;
   c.restitution = cfg.coefficient_of_restitution;
   c.friction = cfg.coefficient_of_friction;
+  c.one = 1.0f;
   c.n_obstacle_faces = n_faces;
   c.obstacle_faces = faces;
   c.flags = flags;

@@ -6,11 +6,15 @@
 // -fmad=false so no a*b+c is fused, and '/' and sqrt are the IEEE-rounded
 // operations; with the same operation order the results are bit-identical to
 // the reference's f32 arithmetic except where a libm function (atan2f) is
-// involved.
+// involved (angle.cuh).
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#if defined(__CUDACC__)
+#include "angle.cuh"
+#endif
 
 namespace fgb {
 
@@ -47,15 +51,19 @@ template <class T> __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
 }
 __device__ __forceinline__ float sq_root(float v) { return sqrtf(v); }
 __device__ __forceinline__ double sq_root(double v) { return sqrt(v); }
-__device__ __forceinline__ float arc_tan2(float y, float x) { return atan2f(y, x); }
-__device__ __forceinline__ double arc_tan2(double y, double x) { return atan2(y, x); }
+// atan2(y, x) for y >= 0 (the angle between two vectors, see vangle): the
+// f32 form is angle.cuh's, the f64 form (the FP64 rerun) libm's.
+#if defined(__CUDACC__)
+__device__ __forceinline__ float angle_of(float y, float x) { return angle_pos(y, x); }
+__device__ __forceinline__ double angle_of(double y, double x) { return atan2(y, x); }
+#endif
 __device__ __forceinline__ float abs_val(float v) { return fabsf(v); }
 __device__ __forceinline__ double abs_val(double v) { return fabs(v); }
 __device__ __forceinline__ float min_num(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ double min_num(double a, double b) { return fmin(a, b); }
 template <class T> __device__ __forceinline__ T magnitude(V3<T> v) { return sq_root(dot(v, v)); }
 template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return v * (T(1) / magnitude(v)); }
-template <class T> __device__ __forceinline__ T vangle(V3<T> a, V3<T> b) { return arc_tan2(magnitude(cross(a, b)), dot(a, b)); }
+template <class T> __device__ __forceinline__ T vangle(V3<T> a, V3<T> b) { return angle_of(magnitude(cross(a, b)), dot(a, b)); }
 template <class T> __device__ __forceinline__ bool is_zero(V3<T> v) { return v.x == T(0) && v.y == T(0) && v.z == T(0); }
 template <class T> __device__ __forceinline__ bool finite3(V3<T> v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 

@@ -1,0 +1,103 @@
+// Drag + lift and the corner weights of two faces at once (the tiled grid
+// kernel's quad: faces A and B), as the two lanes of packed f32x2
+// arithmetic.  Each lane rounds exactly as the scalar instruction does, so
+// every lane gives the bits of physics.cuh's face_total_force and
+// face_corner_weight for its face (tests/test_gpu_math.py checks this).
+#pragma once
+
+#include "angle.cuh"
+#include "devmath.cuh"
+#include "fastdiv.cuh"
+
+namespace fgb {
+
+// A pair of 3-vectors, lane 0 and lane 1 of packed f32x2 registers: faces A
+// and B of a quad run the same expression sequence, so one packed instruction
+// does each step for both with the roundings of the scalar one.
+struct V3x2 {
+  f2 x, y, z;
+};
+__device__ __forceinline__ V3x2 pk3(V3<float> a, V3<float> b) { return {pk(a.x, b.x), pk(a.y, b.y), pk(a.z, b.z)}; }
+__device__ __forceinline__ V3x2 add3(V3x2 a, V3x2 b) { return {add2(a.x, b.x), add2(a.y, b.y), add2(a.z, b.z)}; }
+__device__ __forceinline__ V3x2 sub3(V3x2 a, V3x2 b) { return {sub2(a.x, b.x), sub2(a.y, b.y), sub2(a.z, b.z)}; }
+// s * v (operator*(T, V3): s * v.x, ...) and v * s: the same products
+__device__ __forceinline__ V3x2 scale3(f2 s, V3x2 v) { return {mul2(s, v.x), mul2(s, v.y), mul2(s, v.z)}; }
+// (x x' + y y') + z z', every sum of products an fma with the unit `one`
+// (angle.cuh: add_p2), so each product and each sum is rounded once
+__device__ __forceinline__ f2 dot3(V3x2 a, V3x2 b, f2 one) {
+  return add_p2(mul2(a.z, b.z), add_p2(mul2(a.x, b.x), mul2(a.y, b.y), one), one);
+}
+__device__ __forceinline__ V3x2 cross3(V3x2 a, V3x2 b, f2 one) {
+  return {rsub_p2(mul2(a.z, b.y), mul2(a.y, b.z), one), rsub_p2(mul2(a.x, b.z), mul2(a.z, b.x), one),
+          rsub_p2(mul2(a.y, b.x), mul2(a.x, b.y), one)};
+}
+__device__ __forceinline__ f2 sqrt2(f2 v) {
+  const float2 u = upk(v);
+  return pk(sqrtf(u.x), sqrtf(u.y));
+}
+__device__ __forceinline__ f2 magnitude3(V3x2 v, f2 one) { return sqrt2(dot3(v, v, one)); }
+
+// a / b for b = 3 or pi in both lanes (div_const_try); ok cleared when a
+// lane needs the IEEE division.
+__device__ __forceinline__ f2 div_const2(f2 a, float b, float y, bool& ok) {
+  const f2 q = mul2(a, dup2(y));
+  const f2 r = fma2(dup2(-b), q, a);
+  const f2 q2 = fma2(r, dup2(y), q);
+  const float2 u = upk(a);
+  ok = ok && div_const_ok(u.x) && div_const_ok(u.y);
+  return q2;
+}
+static __device__ __noinline__ f2 div2_ieee_cold(f2 a, float b) {
+  const float2 u = upk(a);
+  return pk(u.x / b, u.y / b);
+}
+
+// drag + lift (D) and the three corner weights angle_k / PI of two faces
+// (springy_mesh.rs:629-654, 134-172), lane 0 and lane 1.  The corner angles
+// reuse exact identities: |(x2-x0) x (x1-x0)| is bitwise |(x1-x0) x (x2-x0)|,
+// and x0-x1 = -(x1-x0), x1-x2 = -(x2-x1) exactly.  The divisions by 3 and pi
+// take one guard per group of three per face (div_const_try).
+__device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, V3x2 v1, V3x2 v2, V3x2 wind,
+                                            float neg_cd, float neg_lift, float one_rt, float4& DwA, float2& wA,
+                                            float4& DwB, float2& wB) {
+  const f2 one = dup2(one_rt);
+  const V3x2 sum = add3(add3(v0, v1), v2);
+  bool ok = true;
+  V3x2 avg{div_const2(sum.x, 3.0f, kRcp3, ok), div_const2(sum.y, 3.0f, kRcp3, ok),
+           div_const2(sum.z, 3.0f, kRcp3, ok)};
+  if (!ok) avg = V3x2{div2_ieee_cold(sum.x, 3.0f), div2_ieee_cold(sum.y, 3.0f), div2_ieee_cold(sum.z, 3.0f)};
+  const V3x2 rv = sub3(avg, wind);
+  const V3x2 e1 = sub3(x1, x0), e2 = sub3(x2, x0), e3 = sub3(x2, x1);
+  const V3x2 cr = cross3(e1, e2, one);
+  const f2 mag = magnitude3(cr, one);
+  const f2 area = mul2(mag, dup2(0.5f));  // mag / 2, exactly
+  f2 inv;
+  {
+    const float2 m = upk(mag);
+    inv = pk(1.0f / m.x, 1.0f / m.y);
+  }
+  const V3x2 n{mul2(cr.x, inv), mul2(cr.y, inv), mul2(cr.z, inv)};
+  const f2 eff = mul2(area, abs2(dot3(n, rv, one)));
+  const V3x2 drag = scale3(mul2(dup2(neg_cd), eff), rv);
+  const f2 m2 = magnitude3(cross3(n, rv, one), one);
+  const V3x2 lift = scale3(mul2(dup2(neg_lift), eff), V3x2{mul2(rv.x, m2), mul2(rv.y, m2), mul2(rv.z, m2)});
+  const V3x2 D{add_p2(lift.x, drag.x, one), add_p2(lift.y, drag.y, one), add_p2(lift.z, drag.z, one)};
+  const f2 a0 = angle_pos2(mag, dot3(e2, e1, one), one);
+  const f2 a1 = angle_pos2(magnitude3(cross3(e1, e3, one), one), neg2(dot3(e1, e3, one)), one);
+  const f2 a2 = angle_pos2(magnitude3(cross3(e3, e2, one), one), dot3(e3, e2, one), one);
+  bool okw = true;
+  f2 w0 = div_const2(a0, kPiF32, kRcpPi, okw), w1 = div_const2(a1, kPiF32, kRcpPi, okw),
+     w2 = div_const2(a2, kPiF32, kRcpPi, okw);
+  if (!okw) {
+    w0 = div2_ieee_cold(a0, kPiF32);
+    w1 = div2_ieee_cold(a1, kPiF32);
+    w2 = div2_ieee_cold(a2, kPiF32);
+  }
+  const float2 dx = upk(D.x), dy = upk(D.y), dz = upk(D.z), u0 = upk(w0), u1 = upk(w1), u2 = upk(w2);
+  DwA = make_float4(dx.x, dy.x, dz.x, u0.x);
+  DwB = make_float4(dx.y, dy.y, dz.y, u0.y);
+  wA = make_float2(u1.x, u2.x);
+  wB = make_float2(u1.y, u2.y);
+}
+
+}  // namespace fgb

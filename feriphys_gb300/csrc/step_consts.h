@@ -51,6 +51,8 @@ struct StepConsts {
   const void* obstacle_faces;  // ObsFace[n_obstacle_faces], flattened obstacle order
   unsigned* flags;             // bit 0: a stepped vertex went non-finite; bit 1: a staging copy timed out
   ObsAccel accel;              // broad phase over obstacle_faces (enabled = 0: test all faces)
+  float one;                   // 1.0f, set by the host: a unit multiplier the device compiler cannot see as 1
+                               // (face_pair.cuh uses it to keep packed sums of products unfused)
 };
 
 }  // namespace fgb

@@ -12,6 +12,7 @@
 #include <mutex>
 
 #include "fastdiv.cuh"
+#include "face_pair.cuh"
 #include "grid_order.h"
 #include "kernels.h"
 #include "per_device.h"
@@ -114,32 +115,6 @@ __global__ void __launch_bounds__(256) k_step_grid_v1(int R, int C, const float4
 // computed and summed in a second phase that reuses the same buffer; faces
 // come after all struts and use it a third time.
 
-// drag+lift (D) and the three corner weights angle_k / PI of one face.  The
-// corner angles reuse exact identities: |(x2-x0) x (x1-x0)| is bitwise
-// |(x1-x0) x (x2-x0)|, and x0-x1 = -(x1-x0), x1-x2 = -(x2-x1) exactly.
-__device__ __forceinline__ void face_terms(V3<float> x0, V3<float> x1, V3<float> x2, V3<float> v0, V3<float> v1,
-                                           V3<float> v2, V3<float> wind, float neg_cd, float neg_lift,
-                                           float4& Dw0, float2& w12) {
-  const V3<float> sum = (v0 + v1) + v2;
-  const V3<float> avg{div_known_rcp(sum.x, 3.0f, kRcp3), div_known_rcp(sum.y, 3.0f, kRcp3),
-                      div_known_rcp(sum.z, 3.0f, kRcp3)};
-  const V3<float> rv = avg - wind;
-  const V3<float> e1 = x1 - x0, e2 = x2 - x0, e3 = x2 - x1;
-  const V3<float> cr = cross(e1, e2);
-  const float mag = magnitude(cr);
-  const float area = mag / 2.0f;
-  const V3<float> n = cr * (1.0f / mag);
-  const float eff = area * fabsf(dot(n, rv));
-  const V3<float> drag = (neg_cd * eff) * rv;
-  const V3<float> lift = (neg_lift * eff) * (rv * magnitude(cross(n, rv)));
-  const V3<float> D = drag + lift;
-  const float a0 = atan2f(mag, dot(e2, e1));
-  const float a1 = atan2f(magnitude(cross(e1, e3)), -dot(e1, e3));
-  const float a2 = atan2f(magnitude(cross(e3, e2)), dot(e3, e2));
-  Dw0 = make_float4(D.x, D.y, D.z, div_known_rcp(a0, kPiF32, kRcpPi));
-  w12 = make_float2(div_known_rcp(a1, kPiF32, kRcpPi), div_known_rcp(a2, kPiF32, kRcpPi));
-}
-
 template <int TW, int TH>
 struct TileGeom {
   static constexpr int EW = TW + 4, EH = TH + 4;  // staged region, origin (r0-2, c0-2)
@@ -203,14 +178,17 @@ __device__ __forceinline__ void add_compact(V3<float>& F, float4 su, float s2, i
 
 __device__ __forceinline__ void quad_to(const float4* __restrict__ s_pos, const float4* __restrict__ s_vel, int e00,
                                         int e01, int e10, int e11, V3<float> wind, float neg_cd, float neg_lift,
+                                        float one,
                                         float4* __restrict__ qa, float4* __restrict__ qb, float4* __restrict__ qw) {
   float4 a, b;
   float2 wa, wb;
-  // A = (i+1, i+C, i), B = (i+1, i+C+1, i+C) for quad origin i
-  face_terms(xyz<float>(s_pos[e01]), xyz<float>(s_pos[e10]), xyz<float>(s_pos[e00]), xyz<float>(s_vel[e01]),
-             xyz<float>(s_vel[e10]), xyz<float>(s_vel[e00]), wind, neg_cd, neg_lift, a, wa);
-  face_terms(xyz<float>(s_pos[e01]), xyz<float>(s_pos[e11]), xyz<float>(s_pos[e10]), xyz<float>(s_vel[e01]),
-             xyz<float>(s_vel[e11]), xyz<float>(s_vel[e10]), wind, neg_cd, neg_lift, b, wb);
+  // A = (i+1, i+C, i), B = (i+1, i+C+1, i+C) for quad origin i: lane 0 face A, lane 1 face B
+  const V3<float> p00 = xyz<float>(s_pos[e00]), p01 = xyz<float>(s_pos[e01]), p10 = xyz<float>(s_pos[e10]),
+                  p11 = xyz<float>(s_pos[e11]);
+  const V3<float> u00 = xyz<float>(s_vel[e00]), u01 = xyz<float>(s_vel[e01]), u10 = xyz<float>(s_vel[e10]),
+                  u11 = xyz<float>(s_vel[e11]);
+  face_terms2(pk3(p01, p01), pk3(p10, p11), pk3(p00, p10), pk3(u01, u01), pk3(u10, u11), pk3(u00, u10),
+              pk3(wind, wind), neg_cd, neg_lift, one, a, wa, b, wb);
   *qa = a;
   *qb = b;
   *qw = make_float4(wa.x, wa.y, wb.x, wb.y);
@@ -415,7 +393,7 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
   }
   if (quad_r > -3)
     quad_to(s_pos, s_vel, e(quad_r, quad_c), e(quad_r, quad_c + 1), e(quad_r + 1, quad_c), e(quad_r + 1, quad_c + 1),
-            wind, c.neg_drag, c.neg_lift, s_qa + qi(quad_r, quad_c), s_qb + qi(quad_r, quad_c),
+            wind, c.neg_drag, c.neg_lift, c.one, s_qa + qi(quad_r, quad_c), s_qb + qi(quad_r, quad_c),
             s_qw + qi(quad_r, quad_c));
   __syncthreads();
   if (vertex) {

@@ -1,10 +1,18 @@
-"""The step's correctly rounded division by a known reciprocal
-(feriphys_gb300/csrc/fastdiv.cuh) returns exactly the IEEE quotient.
+"""The step's own math routines on the GPU.
 
-Checked on the GPU for every one of the 2^32 float numerators with the two
-constant divisors the step uses (3 for the mean face velocity, pi for the
-corner-angle weights), and for 2^30 random (numerator, divisor) pairs as in
-the F/m of the integration.
+* The correctly rounded division by a known reciprocal
+  (feriphys_gb300/csrc/fastdiv.cuh) returns exactly the IEEE quotient: for
+  every one of the 2^32 float numerators with the two constant divisors the
+  step uses (3 for the mean face velocity, pi for the corner-angle weights),
+  both div_known_rcp and the grouped-guard div_const_try wherever its guard
+  accepts the operand, and for 2^30 random (numerator, divisor) pairs as in
+  the F/m of the integration.
+* The packed face pair (face_pair.cuh) gives lane by lane the bits of the
+  scalar face terms (physics.cuh) on 2^22 random quads.
+* The corner angle atan2(y, x), y >= 0 (feriphys_gb300/csrc/angle.cuh) stays
+  within 3 ulp of a double-precision atan2 rounded to f32 over 2^28 random
+  (y, x) pairs spread over many binades and over the special operands, and
+  its packed two-lane form gives the scalar form's bits.
 """
 import ctypes as C
 import os
@@ -19,19 +27,32 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 KERNEL = r"""
 #include <cstdint>
+#include "angle.cuh"
+#include "face_pair.cuh"
 #include "fastdiv.cuh"
+#include "physics.cuh"
 using namespace fgb;
 __device__ __forceinline__ bool same(float x, float y) {
   return (__float_as_uint(x) == __float_as_uint(y)) || (isnan(x) && isnan(y));
 }
-__global__ void all_numerators(float b, float y, unsigned long long* bad) {
-  unsigned long long local = 0;
+__global__ void all_numerators(float b, float y, unsigned long long* bad, unsigned long long* bad_try,
+                               unsigned long long* taken) {
+  unsigned long long local = 0, local_try = 0, local_taken = 0;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32);
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const float a = __uint_as_float(unsigned(i));
-    if (!same(div_known_rcp(a, b, y), __fdiv_rn(a, b))) ++local;
+    const float ref = __fdiv_rn(a, b);
+    if (!same(div_known_rcp(a, b, y), ref)) ++local;
+    bool ok = true;
+    const float q = div_const_try(a, b, y, ok);
+    if (ok) {
+      ++local_taken;
+      if (!same(q, ref)) ++local_try;
+    }
   }
   if (local) atomicAdd(bad, local);
+  if (local_try) atomicAdd(bad_try, local_try);
+  atomicAdd(taken, local_taken);
 }
 __device__ __forceinline__ unsigned mix(unsigned long long x) {
   x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
@@ -49,13 +70,124 @@ __global__ void random_pairs(unsigned long long n, unsigned long long* bad) {
   }
   if (local) atomicAdd(bad, local);
 }
+// ulp distance of two finite floats of the same sign (order-preserving integers)
+__device__ __forceinline__ long long ordered(float x) {
+  const int i = __float_as_int(x);
+  return i >= 0 ? (long long)i : -(long long)(i & 0x7fffffff);
+}
+__global__ void angles(unsigned long long n, unsigned long long* worst_ulp, unsigned long long* bad_pair,
+                       unsigned long long* n_fast, float one) {
+  unsigned long long worst = 0, badp = 0, fast = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    // y >= 0 and x of either sign, magnitudes over 2^-40 .. 2^40, with every 64th pair exactly special
+    const unsigned ry = mix(3 * i), rx = mix(3 * i + 1), rs = mix(3 * i + 2);
+    float y = __uint_as_float(0x2b800000u + ry % 0x28000000u);
+    float x = __uint_as_float((rx & 0x80000000u) | (0x2b800000u + (rx >> 1) % 0x28000000u));
+    switch (rs & 63) {
+      case 0: y = 0.0f; break;
+      case 1: x = 0.0f; break;
+      case 2: x = -0.0f; break;
+      case 3: y = x = 0.0f; break;
+      case 4: x = __uint_as_float(0x7f800000u); break;
+      case 5: y = __uint_as_float(0x7f800000u); break;
+      case 6: x = -y; break;
+      case 7: x = y; break;
+      default: break;
+    }
+    const float got = angle_pos(y, x);
+    const float ref = (float)atan2((double)y, (double)x);
+    const long long d = ordered(got) - ordered(ref);
+    const unsigned long long u = (unsigned long long)(d < 0 ? -d : d);
+    if (u > worst) worst = u;
+    if (angle_detail::in_range(y, x)) ++fast;
+    // the packed form, lane 0 and lane 1 with different operands
+    const float y2 = angle_pos(x < 0.0f ? -x : x, y);
+    const float2 p = upk(angle_pos2(pk(y, x < 0.0f ? -x : x), pk(x, y), pk(one, one)));
+    if (!same(p.x, got) || !same(p.y, y2)) ++badp;
+  }
+  atomicMax(worst_ulp, worst);
+  if (badp) atomicAdd(bad_pair, badp);
+  atomicAdd(n_fast, fast);
+}
+extern "C" int run_angles(unsigned long long n, unsigned long long* out) {
+  unsigned long long* d;
+  if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return -1;
+  cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+  angles<<<4096, 256>>>(n, d, d + 1, d + 2, 1.0f);
+  if (cudaMemcpy(out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+  cudaFree(d);
+  return 0;
+}
+// Packed face pairs against the scalar face terms of the general kernels:
+// random cloth-like triangles (a unit-spaced corner set jittered, scaled
+// over many binades), velocities (some exactly zero) and wind.
+__device__ __forceinline__ float unit(unsigned r) { return (r >> 8) * (1.0f / 16777216.0f) * 2.0f - 1.0f; }
+__global__ void face_pairs(unsigned long long n, unsigned long long* bad, float* first, float one) {
+  unsigned long long badl = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long k = 40 * i;
+    const float sc = exp2f(float(int(mix(k++) % 24u)) - 12.0f);
+    V3<float> x[4], v[4];
+    const float cx[4] = {0, 1, 0, 1}, cy[4] = {0, 0, 1, 1};
+    for (int j = 0; j < 4; ++j) {
+      x[j] = V3<float>{sc * (cx[j] + 0.3f * unit(mix(k++))), sc * (cy[j] + 0.3f * unit(mix(k++))),
+                       (i & 7) == 0 ? 0.0f : sc * 0.3f * unit(mix(k++))};
+      const bool still = (i & 15) == 1;
+      v[j] = V3<float>{still ? 0.0f : 3.0f * unit(mix(k++)), still ? 0.0f : 3.0f * unit(mix(k++)),
+                       still ? 0.0f : 3.0f * unit(mix(k++))};
+    }
+    const V3<float> wind{2.0f * unit(mix(k++)), 2.0f * unit(mix(k++)), 2.0f * unit(mix(k++))};
+    const float ncd = -0.6f, ncl = -0.3f;
+    // quad corners 00 = x[0], 01 = x[1], 10 = x[2], 11 = x[3]; A = (01, 10, 00), B = (01, 11, 10)
+    float4 DA, DB;
+    float2 wA, wB;
+    face_terms2(pk3(x[1], x[1]), pk3(x[2], x[3]), pk3(x[0], x[2]), pk3(v[1], v[1]), pk3(v[2], v[3]),
+                pk3(v[0], v[2]), pk3(wind, wind), ncd, ncl, one, DA, wA, DB, wB);
+    const int tri[2][3] = {{1, 2, 0}, {1, 3, 2}};
+    const float got[2][6] = {{DA.x, DA.y, DA.z, DA.w, wA.x, wA.y}, {DB.x, DB.y, DB.z, DB.w, wB.x, wB.y}};
+    for (int f = 0; f < 2; ++f) {
+      const V3<float> a = x[tri[f][0]], b = x[tri[f][1]], c = x[tri[f][2]];
+      const V3<float> D = face_total_force<float>(a, b, c, v[tri[f][0]], v[tri[f][1]], v[tri[f][2]], wind, ncd, ncl);
+      const float ref[6] = {D.x, D.y, D.z, face_corner_weight<float>(a, b, c, 0),
+                            face_corner_weight<float>(a, b, c, 1), face_corner_weight<float>(a, b, c, 2)};
+      for (int q = 0; q < 6; ++q)
+        if (!same(got[f][q], ref[q])) {
+          if (atomicAdd(bad, 1ull) == 0) {
+            first[0] = float(i); first[1] = float(f); first[2] = float(q);
+            first[3] = got[f][q]; first[4] = ref[q];
+            for (int j = 0; j < 3; ++j) {
+              first[5 + 3 * j] = x[tri[f][j]].x; first[6 + 3 * j] = x[tri[f][j]].y; first[7 + 3 * j] = x[tri[f][j]].z;
+            }
+          }
+          ++badl;
+          break;
+        }
+    }
+  }
+}
+extern "C" int run_faces(unsigned long long n, unsigned long long* out, float* first) {
+  unsigned long long* d;
+  float* df;
+  if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return -1;
+  if (cudaMalloc(&df, 16 * sizeof(float)) != cudaSuccess) return -1;
+  cudaMemset(d, 0, sizeof(unsigned long long));
+  cudaMemset(df, 0, 16 * sizeof(float));
+  face_pairs<<<1024, 256>>>(n, d, df, 1.0f);
+  if (cudaMemcpy(out, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+  cudaMemcpy(first, df, 16 * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(df);
+  return 0;
+}
 extern "C" int run(float b, float y, unsigned long long n_random, unsigned long long* out) {
   unsigned long long* d;
-  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return -1;
-  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
-  all_numerators<<<4096, 256>>>(b, y, d);
+  if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return -1;
+  cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  all_numerators<<<4096, 256>>>(b, y, d, d + 2, d + 3);
   random_pairs<<<4096, 256>>>(n_random, d + 1);
-  if (cudaMemcpy(out, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+  if (cudaMemcpy(out, d, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
   cudaFree(d);
   return 0;
 }
@@ -73,12 +205,35 @@ def divlib():
                            "-o", lib, src])
     l = C.CDLL(lib)
     l.run.argtypes = [C.c_float, C.c_float, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
+    l.run_angles.argtypes = [C.c_ulonglong, C.POINTER(C.c_ulonglong)]
+    l.run_faces.argtypes = [C.c_ulonglong, C.POINTER(C.c_ulonglong), C.POINTER(C.c_float)]
     return l
 
 
 @pytest.mark.parametrize("b,y", [(3.0, 0.333333343267440796), (3.14159265358979323846, 0.318309873342514038)])
 def test_division_exact(divlib, b, y):
-    out = (C.c_ulonglong * 2)()
+    out = (C.c_ulonglong * 4)()
     assert divlib.run(b, y, 1 << 30, out) == 0
     assert out[0] == 0, "%d numerators differ from IEEE division by %r" % (out[0], b)
     assert out[1] == 0, "%d random pairs differ from IEEE division" % out[1]
+    assert out[2] == 0, "%d numerators accepted by div_const_try differ from IEEE division by %r" % (out[2], b)
+    assert out[3] > (1 << 31), out[3]  # the guard accepts the bulk of the finite range
+
+
+def test_angle_accuracy_and_pairs(divlib):
+    out = (C.c_ulonglong * 3)()
+    n = 1 << 28
+    assert divlib.run_angles(n, out) == 0
+    print("angle: worst %d ulp, %d of %d on the fast path" % (out[0], out[2], n))
+    assert out[0] <= 3, "angle_pos is %d ulp from atan2 in double" % out[0]
+    assert out[1] == 0, "%d packed results differ from the scalar ones" % out[1]
+    assert out[2] > n // 2
+
+
+def test_face_pairs_match_scalar_faces(divlib):
+    """The tiled kernel's packed face pair gives, lane by lane, the bits of
+    the scalar face terms the general and untiled kernels use."""
+    out = (C.c_ulonglong * 1)()
+    first = (C.c_float * 16)()
+    assert divlib.run_faces(1 << 22, out, first) == 0
+    assert out[0] == 0, "%d faces differ; first: %s" % (out[0], list(first))
