@@ -14,6 +14,7 @@
 
 #if defined(__CUDACC__)
 #include "angle.cuh"
+#include "fastdiv.cuh"
 #endif
 
 namespace fgb {
@@ -56,13 +57,17 @@ __device__ __forceinline__ double sq_root(double v) { return sqrt(v); }
 #if defined(__CUDACC__)
 __device__ __forceinline__ float angle_of(float y, float x) { return angle_pos(y, x); }
 __device__ __forceinline__ double angle_of(double y, double x) { return atan2(y, x); }
+// 1 / |v| for normalize: the f32 form without the IEEE reciprocal's range
+// branch (fastdiv.cuh: rcp_of_root, the same bits)
+__device__ __forceinline__ float inv_magnitude(float m) { return rcp_of_root(m); }
+__device__ __forceinline__ double inv_magnitude(double m) { return 1.0 / m; }
 #endif
 __device__ __forceinline__ float abs_val(float v) { return fabsf(v); }
 __device__ __forceinline__ double abs_val(double v) { return fabs(v); }
 __device__ __forceinline__ float min_num(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ double min_num(double a, double b) { return fmin(a, b); }
 template <class T> __device__ __forceinline__ T magnitude(V3<T> v) { return sq_root(dot(v, v)); }
-template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return v * (T(1) / magnitude(v)); }
+template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return v * inv_magnitude(magnitude(v)); }
 template <class T> __device__ __forceinline__ T vangle(V3<T> a, V3<T> b) { return angle_of(magnitude(cross(a, b)), dot(a, b)); }
 template <class T> __device__ __forceinline__ bool is_zero(V3<T> v) { return v.x == T(0) && v.y == T(0) && v.z == T(0); }
 template <class T> __device__ __forceinline__ bool finite3(V3<T> v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }

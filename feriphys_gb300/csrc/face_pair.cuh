@@ -36,6 +36,14 @@ __device__ __forceinline__ f2 sqrt2(f2 v) {
   return pk(sqrtf(u.x), sqrtf(u.y));
 }
 __device__ __forceinline__ f2 magnitude3(V3x2 v, f2 one) { return sqrt2(dot3(v, v, one)); }
+// rcp_of_root (fastdiv.cuh) in both lanes: 1 / magnitude with the bits of 1/x
+__device__ __forceinline__ f2 rcp_of_root2(f2 x) {
+  const float2 u = upk(x);
+  const f2 y0 = pk(rcp_approx_ftz(u.x), rcp_approx_ftz(u.y));
+  const f2 e = fma2(neg2(x), y0, dup2(1.0f));
+  const float2 y1 = upk(fma2(y0, e, y0)), z = upk(y0);
+  return pk(y1.x != y1.x ? z.x : y1.x, y1.y != y1.y ? z.y : y1.y);
+}
 
 // a / b for b = 3 or pi in both lanes (div_const_try); ok cleared when a
 // lane needs the IEEE division.
@@ -71,11 +79,7 @@ __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, 
   const V3x2 cr = cross3(e1, e2, one);
   const f2 mag = magnitude3(cr, one);
   const f2 area = mul2(mag, dup2(0.5f));  // mag / 2, exactly
-  f2 inv;
-  {
-    const float2 m = upk(mag);
-    inv = pk(1.0f / m.x, 1.0f / m.y);
-  }
+  const f2 inv = rcp_of_root2(mag);
   const V3x2 n{mul2(cr.x, inv), mul2(cr.y, inv), mul2(cr.z, inv)};
   const f2 eff = mul2(area, abs2(dot3(n, rv, one)));
   const V3x2 drag = scale3(mul2(dup2(neg_cd), eff), rv);

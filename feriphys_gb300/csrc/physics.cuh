@@ -59,7 +59,7 @@ struct MassDiv {
 };
 __device__ __forceinline__ MassDiv mass_div(float m) {
   const bool fast = rcp_usable(m);
-  return {m, fast ? __frcp_rn(m) : 0.0f, fast};
+  return {m, fast ? rcp_rn_fast(m) : 0.0f, fast};
 }
 static __device__ __noinline__ V3<float> div3_ieee_cold(V3<float> F, float m) { return F / m; }
 __device__ __forceinline__ V3<float> div_mass(V3<float> F, float m, const MassDiv& d) {

@@ -158,7 +158,7 @@ __device__ __forceinline__ void strut_compact(const float4* __restrict__ s_pos, 
                                               float* __restrict__ s2) {
   const V3<float> d = xyz<float>(s_pos[ib]) - xyz<float>(s_pos[ia]);
   const float mag = magnitude(d);
-  const V3<float> u = d * (1.0f / mag);
+  const V3<float> u = d * rcp_of_root(mag);  // 1 / mag, the IEEE bits
   const float s1 = k * (mag - L);
   const float sd = cd * dot(xyz<float>(s_vel[ib]) - xyz<float>(s_vel[ia]), u);
   *su = make_float4(u.x, u.y, u.z, s1);

@@ -7,6 +7,9 @@
   both div_known_rcp and the grouped-guard div_const_try wherever its guard
   accepts the operand, and for 2^30 random (numerator, divisor) pairs as in
   the F/m of the integration.
+* The branch-free reciprocals (fastdiv.cuh) equal the IEEE 1/x: rcp_rn_fast
+  for every float of magnitude [2^-124, 2^124), rcp_of_root and its packed
+  form for the square root of every float.
 * The packed face pair (face_pair.cuh) gives lane by lane the bits of the
   scalar face terms (physics.cuh) on 2^22 random quads.
 * The corner angle atan2(y, x), y >= 0 (feriphys_gb300/csrc/angle.cuh) stays
@@ -181,6 +184,39 @@ extern "C" int run_faces(unsigned long long n, unsigned long long* out, float* f
   cudaFree(df);
   return 0;
 }
+// The branch-free reciprocals: rcp_rn_fast for every float of magnitude
+// [2^-124, 2^124), either sign; rcp_of_root (and its packed form, with a
+// second root in the other lane) for the square root of every float.
+__global__ void reciprocals(unsigned long long* bad_fast, unsigned long long* bad_root,
+                            unsigned long long* bad_pair, unsigned long long* n_fast) {
+  unsigned long long bf = 0, br = 0, bp = 0, nf = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32);
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const float x = __uint_as_float(unsigned(i));
+    const unsigned e = (unsigned(i) >> 23) & 0xffu;
+    if (e >= 3 && e <= 250) {
+      ++nf;
+      if (!same(rcp_rn_fast(x), __fdiv_rn(1.0f, x))) ++bf;
+    }
+    const float m = __fsqrt_rn(x), m2 = __fsqrt_rn(__uint_as_float(unsigned(i) ^ 0x00400000u));
+    if (!same(rcp_of_root(m), __fdiv_rn(1.0f, m))) ++br;
+    const float2 p = upk(rcp_of_root2(pk(m, m2)));
+    if (!same(p.x, __fdiv_rn(1.0f, m)) || !same(p.y, __fdiv_rn(1.0f, m2))) ++bp;
+  }
+  if (bf) atomicAdd(bad_fast, bf);
+  if (br) atomicAdd(bad_root, br);
+  if (bp) atomicAdd(bad_pair, bp);
+  atomicAdd(n_fast, nf);
+}
+extern "C" int run_reciprocals(unsigned long long* out) {
+  unsigned long long* d;
+  if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return -1;
+  cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  reciprocals<<<4096, 256>>>(d, d + 1, d + 2, d + 3);
+  if (cudaMemcpy(out, d, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+  cudaFree(d);
+  return 0;
+}
 extern "C" int run(float b, float y, unsigned long long n_random, unsigned long long* out) {
   unsigned long long* d;
   if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return -1;
@@ -207,6 +243,7 @@ def divlib():
     l.run.argtypes = [C.c_float, C.c_float, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
     l.run_angles.argtypes = [C.c_ulonglong, C.POINTER(C.c_ulonglong)]
     l.run_faces.argtypes = [C.c_ulonglong, C.POINTER(C.c_ulonglong), C.POINTER(C.c_float)]
+    l.run_reciprocals.argtypes = [C.POINTER(C.c_ulonglong)]
     return l
 
 
@@ -237,3 +274,15 @@ def test_face_pairs_match_scalar_faces(divlib):
     first = (C.c_float * 16)()
     assert divlib.run_faces(1 << 22, out, first) == 0
     assert out[0] == 0, "%d faces differ; first: %s" % (out[0], list(first))
+
+
+def test_reciprocals_exact(divlib):
+    """rcp_rn_fast is the IEEE reciprocal on its whole stated range, and
+    rcp_of_root (scalar and packed) is 1/x for every square root a float can
+    have, zeros, infinity and NaN included."""
+    out = (C.c_ulonglong * 4)()
+    assert divlib.run_reciprocals(out) == 0
+    assert out[0] == 0, "%d operands of rcp_rn_fast differ from 1/x" % out[0]
+    assert out[1] == 0, "%d square roots where rcp_of_root differs from 1/x" % out[1]
+    assert out[2] == 0, "%d square roots where the packed rcp_of_root2 differs from 1/x" % out[2]
+    assert out[3] == 2 * 248 * (1 << 23), out[3]
