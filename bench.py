@@ -46,6 +46,7 @@ sys.path.insert(0, ROOT)
 METRIC = "cloth vertex-steps/s"
 UNIT = "vertex-steps/s"
 KERNEL_PROFILE = os.path.join(ROOT, "profiles", "step_grid_c1.md")
+GENERAL_PROFILE = os.path.join(ROOT, "profiles", "step_general_c1.md")
 
 
 def algorithmic_bytes_per_vertex_step(n_vertices: int, n_struts: int) -> float:
@@ -82,13 +83,13 @@ def profile_figure(path, key):
     return float(m.group(1)) if m else None
 
 
-def profile_traffic():
+def profile_traffic(path=KERNEL_PROFILE, key="dram_bytes_per_launch"):
     """DRAM bytes per launch of the step kernel from the committed ncu summary."""
     try:
-        txt = open(KERNEL_PROFILE).read()
+        txt = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    m = re.search(key + r":\s*([0-9.eE+]+)", txt)
     return float(m.group(1)) if m else None
 
 
@@ -680,7 +681,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="c1 only: leave out the batched (c2) and batched-surrogate (c4) results of the line")
-    ap.add_argument("--path", type=int, default=0, help="0 auto, 1 general gather, 2 tiled grid, 3 untiled grid")
+    ap.add_argument("--path", type=int, default=0,
+                    help="0 auto, 1 general gather, 2 tiled grid, 3 untiled grid, 4 general gather (plain lists)")
     ap.add_argument("--probe", action="store_true", help="report the first step whose state is non-finite")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
                     help="c1: one 1024x1024 cloth (default); c2: 4096 uneven cloths, one launch per step; "
@@ -865,7 +867,10 @@ def main():
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     B = algorithmic_bytes_per_vertex_step(n_vert, n_struts)
     achieved = B * n_vert / (ms_step * 1e-3) / 1e9
-    traffic = profile_traffic()
+    # DRAM bytes per launch of the 1024^2 step from the committed ncu summaries
+    path_used = args.path if args.path in (3, 4) else mesh.get_path()
+    traffic = {2: profile_traffic(), 1: profile_traffic(GENERAL_PROFILE),
+               4: profile_traffic(GENERAL_PROFILE, "dram_bytes_per_launch_plain")}.get(path_used) if args.n == 1024 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "algorithmic_bytes_per_launch": B * n_vert,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
@@ -936,7 +941,8 @@ def main():
                 "config": {"workload": c1_workload(args.n, args.rollout),
                            "l2": "flushed (256 MB write) before every timed step",
                            "parallelism": "replicas" if world > 1 else "single GPU",
-                           "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil"}[3 if args.path == 3 else mesh.get_path()]},
+                           "path": {1: "general gather", 2: "tiled grid stencil", 3: "untiled grid stencil",
+                                    4: "general gather (plain lists)"}[path_used]},
                 "ms_per_step_median": ms_median,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_positions": e2e_positions,
                 "parity": parity, "around_the_step": around,

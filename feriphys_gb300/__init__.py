@@ -361,7 +361,8 @@ class SpringyMesh:
         _check(_lib().fgb_mesh_set_strut_params(self._h, _ptr(k), _ptr(c)))
 
     def set_path(self, path: int):
-        """0 auto, 1 general gather, 2 grid (32x8 tiles), 3 grid (one thread per vertex)."""
+        """0 auto, 1 general gather, 2 grid (32x8 tiles), 3 grid (one thread per vertex),
+        4 general gather over the plain incidence lists."""
         _check(_lib().fgb_mesh_set_path(self._h, int(path)))
 
     def get_path(self) -> int:

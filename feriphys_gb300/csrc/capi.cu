@@ -136,6 +136,14 @@ void free_topology(fgb_mesh* m) {
   dfree(m->d_face_off);
   dfree(m->d_face_inc);
   dfree(m->d_face_vtx);
+  dfree(m->d_own_off);
+  dfree(m->d_sk);
+  dfree(m->d_sc);
+  dfree(m->d_sl);
+  dfree(m->d_strut_word);
+  dfree(m->d_strut_word16);
+  dfree(m->d_face_word);
+  m->compact_form = 0;
   dfree(m->d_grid);
   dfree(m->d_rest);
   m->csr_ready = false;
@@ -238,8 +246,42 @@ int ensure_csr(fgb_mesh* m) {
   FGB_CUDA(cudaMemcpy(m->d_face_off, t.face_off.data(), t.face_off.size() * sizeof(int), cudaMemcpyHostToDevice));
   FGB_CUDA(cudaMemcpy(m->d_face_inc, t.face_inc.data(), t.face_inc.size() * sizeof(int), cudaMemcpyHostToDevice));
   FGB_CUDA(cudaMemcpy(m->d_face_vtx, t.face_vtx.data(), t.face_vtx.size() * sizeof(int), cudaMemcpyHostToDevice));
+  fgb::CompactTopo ct;
+  if (fgb::build_compact(m->topo, t, ct)) {
+    auto up = [&](auto*& d, const auto& v) -> cudaError_t {
+      const size_t bytes = v.size() * sizeof(v[0]);
+      cudaError_t e = dalloc(d, bytes);
+      if (e == cudaSuccess && bytes) e = cudaMemcpy(d, v.data(), bytes, cudaMemcpyHostToDevice);
+      return e;
+    };
+    FGB_CUDA(up(m->d_own_off, ct.own_off));
+    FGB_CUDA(up(m->d_sk, ct.sk));
+    FGB_CUDA(up(m->d_sc, ct.sc));
+    FGB_CUDA(up(m->d_sl, ct.sl));
+    FGB_CUDA(ct.strut_word16.size() || ct.strut_word.empty() ? up(m->d_strut_word16, ct.strut_word16)
+                                                              : up(m->d_strut_word, ct.strut_word));
+    FGB_CUDA(up(m->d_face_word, ct.face_word));
+    m->compact_form = ct.strut_word.empty() ? 2 : 1;
+  }
   m->csr_ready = true;
   return FGB_OK;
+}
+
+// The general gather's topology: the compact lists when the mesh has them
+// (and the caller has not asked for the plain CSR), else the plain CSR.
+fgb::GeneralTopo general_topo(const fgb_mesh* m) {
+  fgb::GeneralTopo t{m->d_strut_off, m->d_strut_inc, m->d_strut_kcl, m->d_face_off, m->d_face_inc, m->d_face_vtx};
+  if (m->compact_form && !m->plain_csr) {
+    t.form = m->compact_form;
+    t.own_off = m->d_own_off;
+    t.sk = m->d_sk;
+    t.sc = m->d_sc;
+    t.sl = m->d_sl;
+    t.strut_word = m->d_strut_word;
+    t.strut_word16 = m->d_strut_word16;
+    t.face_word = m->d_face_word;
+  }
+  return t;
 }
 
 // Path choice (host only): 2 = grid kernel, 1 = general gather.
@@ -326,7 +368,7 @@ int step_mesh(fgb_mesh* m, const fgb::StepConsts& c) {
                                    static_cast<float4*>(m->pos[nxt]), static_cast<float4*>(m->vel[nxt]), c,
                                    m->stream));
   } else {
-    fgb::GeneralTopo t{m->d_strut_off, m->d_strut_inc, m->d_strut_kcl, m->d_face_off, m->d_face_inc, m->d_face_vtx};
+    const fgb::GeneralTopo t = general_topo(m);
     if (m->precision == 64)
       FGB_CUDA(fgb::launch_step_general<double>(n, m->pos[m->cur], m->vel[m->cur], F, m->pos[nxt], m->vel[nxt], t,
                                                 c, m->stream));
@@ -969,9 +1011,10 @@ int fgb_mesh_export_indices(fgb_mesh* m, void* device_out, void* stream) {
 }
 
 int fgb_mesh_set_path(fgb_mesh* m, int path) {
-  if (!m || path < 0 || path > 3) return fail(FGB_EINVAL, "path must be 0, 1, 2 or 3");
-  m->path_req = path == 3 ? 2 : path;
+  if (!m || path < 0 || path > 4) return fail(FGB_EINVAL, "path must be 0, 1, 2, 3 or 4");
+  m->path_req = path == 3 ? 2 : (path == 4 ? 1 : path);
   m->grid_variant = path == 3 ? 1 : 0;
+  m->plain_csr = path == 4;
   m->topo_dirty = true;
   return FGB_OK;
 }
@@ -1003,7 +1046,7 @@ int fgb_mesh_accumulate_forces(fgb_mesh* m, const fgb_config* cfg) {
   FGB_CHECK_RC(ensure_csr(m));
   FGB_CHECK_RC(ensure_force(m));
   const fgb::StepConsts c = make_consts(*cfg, nullptr, 0, m->d_flags);
-  fgb::GeneralTopo t{m->d_strut_off, m->d_strut_inc, m->d_strut_kcl, m->d_face_off, m->d_face_inc, m->d_face_vtx};
+  const fgb::GeneralTopo t = general_topo(m);
   if (m->precision == 64)
     FGB_CUDA(fgb::launch_accumulate<double>(int(m->topo.n), m->pos[m->cur], m->vel[m->cur], m->force, t, c, m->stream));
   else

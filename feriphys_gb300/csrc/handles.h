@@ -40,6 +40,7 @@ struct fgb_mesh {
   int device = 0;
   int path_req = 0;      // 0 auto, 1 general, 2 grid
   int grid_variant = 0;  // 0 tiled grid kernel, 1 per-vertex grid kernel
+  bool plain_csr = false;  // general gather over the plain CSR even when the compact lists exist
   int precision = 32;    // 32 or 64
   int active_path = 0;   // 1 general, 2 grid (valid after topology upload)
   cudaStream_t stream = nullptr;      // the stream all work of this mesh is issued on
@@ -78,6 +79,15 @@ struct fgb_mesh {
   int* d_face_off = nullptr;
   int* d_face_inc = nullptr;
   int4* d_face_vtx = nullptr;
+  // its compact form (null when the mesh does not fit it)
+  int* d_own_off = nullptr;
+  float* d_sk = nullptr;
+  float* d_sc = nullptr;
+  float* d_sl = nullptr;
+  uint32_t* d_strut_word = nullptr;
+  uint16_t* d_strut_word16 = nullptr;
+  uint16_t* d_face_word = nullptr;
+  int compact_form = 0;  // 0 none, 1 32-bit strut words, 2 16-bit strut words
   // grid topology
   float4* d_grid = nullptr;
   float4* d_rest = nullptr;  // construction positions (x, y, z, 0), uploaded for the surrogate's inputs

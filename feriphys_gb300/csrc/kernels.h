@@ -17,6 +17,16 @@ struct GeneralTopo {
   const int* face_off;
   const int* face_inc;
   const int4* face_vtx;
+  // the compact form (mesh_build.h: CompactTopo): form 1 with 32-bit strut
+  // words, 2 with 16-bit ones; form 0 reads the lists above instead
+  int form = 0;
+  const int* own_off = nullptr;
+  const float* sk = nullptr;
+  const float* sc = nullptr;
+  const float* sl = nullptr;
+  const uint32_t* strut_word = nullptr;
+  const uint16_t* strut_word16 = nullptr;
+  const uint16_t* face_word = nullptr;
 };
 
 // Grid (Cloth::new topology) description for the stencil kernel (see

@@ -363,6 +363,80 @@ int build_csr(const MeshTopo& m, CsrTopo& t, std::string& err) {
   return FGB_OK;
 }
 
+bool build_compact(const MeshTopo& m, const CsrTopo& t, CompactTopo& out) {
+  out = CompactTopo{};
+  const uint32_t n = m.n;
+  const size_t S = m.sa.size(), F = m.fv.size() / 3;
+  std::vector<int> own_off(size_t(n) + 1, 0);
+  for (size_t s = 0; s < S; ++s) own_off[m.sa[s] + 1]++;
+  for (uint32_t v = 0; v < n; ++v) {
+    if (own_off[v + 1] > 32) return false;  // rank must fit 5 bits
+    own_off[v + 1] += own_off[v];
+  }
+  std::vector<int> fill(own_off.begin(), own_off.end() - 1);
+  std::vector<uint32_t> rank(S);
+  std::vector<float> sk(S), sc(S), sl(S);
+  for (size_t s = 0; s < S; ++s) {  // strut order => each owner range ascends by strut id
+    const uint32_t a = m.sa[s];
+    const int i = fill[a]++;
+    rank[s] = uint32_t(i - own_off[a]);
+    sk[i] = m.sk[s];
+    sc[i] = m.sc[s];
+    sl[i] = m.sl[s];
+  }
+  const int64_t kLim = int64_t(1) << 25;
+  const size_t E = t.strut_inc.size() / 2;
+  std::vector<uint32_t> sw(E);
+  bool fits16 = true;
+  for (uint32_t v = 0; v < n; ++v) {
+    if (t.strut_off[v + 1] - t.strut_off[v] > 127) return false;  // face positions must fit 7 bits
+    for (int e = t.strut_off[v]; e < t.strut_off[v + 1]; ++e) {
+      const int64_t off = int64_t(t.strut_inc[2 * e]) - int64_t(v);
+      if (off <= -kLim || off >= kLim) return false;
+      const uint32_t s = uint32_t(t.strut_inc[2 * e + 1]) >> 1, role = uint32_t(t.strut_inc[2 * e + 1]) & 1u;
+      sw[e] = (uint32_t(int32_t(off)) << 6) | (rank[s] << 1) | role;
+      fits16 = fits16 && (role ? off >= -2048 && off < 2048 && rank[s] < 8 : off >= -16384 && off < 16384);
+    }
+  }
+  std::vector<uint16_t> sw16;
+  if (fits16) {
+    sw16.resize(E);
+    for (size_t e = 0; e < E; ++e) {
+      const int32_t off = int32_t(sw[e]) >> 6;
+      sw16[e] = (sw[e] & 1u) ? uint16_t((uint32_t(off) << 4) | (((sw[e] >> 1) & 7u) << 1) | 1u)
+                             : uint16_t(uint32_t(off) << 1);
+    }
+    sw.clear();
+  }
+  std::vector<uint16_t> fw(t.face_inc.size());
+  for (uint32_t v = 0; v < n; ++v) {
+    const int sb = t.strut_off[v], se = t.strut_off[v + 1];
+    auto pos_of = [&](uint32_t u) -> int {  // first position of neighbour u in v's strut list
+      for (int e = sb; e < se; ++e)
+        if (uint32_t(t.strut_inc[2 * e]) == u) return e - sb;
+      return -1;
+    };
+    for (int e = t.face_off[v]; e < t.face_off[v + 1]; ++e) {
+      const size_t f = size_t(uint32_t(t.face_inc[e]) >> 2);
+      const int corner = t.face_inc[e] & 3;
+      if (f >= F) return false;
+      const uint32_t* fv = &m.fv[3 * f];
+      const uint32_t u1 = corner == 0 ? fv[1] : fv[0], u2 = corner == 2 ? fv[1] : fv[2];
+      const int i1 = pos_of(u1), i2 = pos_of(u2);
+      if (i1 < 0 || i2 < 0) return false;
+      fw[e] = uint16_t(uint32_t(corner) | (uint32_t(i1) << 2) | (uint32_t(i2) << 9));
+    }
+  }
+  out.own_off = std::move(own_off);
+  out.sk = std::move(sk);
+  out.sc = std::move(sc);
+  out.sl = std::move(sl);
+  out.strut_word = std::move(sw);
+  out.strut_word16 = std::move(sw16);
+  out.face_word = std::move(fw);
+  return true;
+}
+
 namespace {
 
 // Strut id of the strut in `slot` of vertex (r, c), or -1 when absent, found

@@ -73,6 +73,39 @@ struct CsrTopo {
 };
 int build_csr(const MeshTopo& m, CsrTopo& out, std::string& err);
 
+// The compact form of the same incidence lists (see step_general.cu), which
+// the step reads instead of strut_inc, strut_kcl, face_inc and face_vtx:
+//   own_off[v]..own_off[v+1]   the struts whose first vertex is v, ascending
+//                              by strut id ("owner order")
+//   sk/sc/sl[i]                stiffness, damping, rest length of the strut
+//                              at owner position i
+//   strut_word[e]              per strut incidence (same order and offsets as
+//                              strut_inc): (other - v) << 6 | rank << 1 | role,
+//                              rank = the strut's position in its first
+//                              vertex's owner range; or, when they fit,
+//   strut_word16[e]            the same in 16 bits (strut_word stays empty):
+//                              role 0: (other - v) << 1, the offset in
+//                              [-16384, 16383] (no rank: v's own struts are
+//                              taken in order); role 1: (other - v) << 4 |
+//                              rank << 1 | 1, the offset in [-2048, 2047] and
+//                              the rank below 8
+//   face_word[e]               per face incidence (same order and offsets as
+//                              face_inc): corner | i1 << 2 | i2 << 9, i1 and i2
+//                              the positions in v's strut list of the face's
+//                              other two vertices, in face order
+// Returns false (and leaves out empty) when the mesh does not fit it: a face
+// vertex that is no strut neighbour, a vertex with more than 127 strut
+// incidences, more than 32 struts owned by one vertex, or a vertex offset
+// beyond +-2^25.
+struct CompactTopo {
+  std::vector<int> own_off;             // n+1
+  std::vector<float> sk, sc, sl;        // S each, owner order
+  std::vector<uint32_t> strut_word;     // one per strut incidence (32-bit form)
+  std::vector<uint16_t> strut_word16;   // one per strut incidence (16-bit form)
+  std::vector<uint16_t> face_word;      // one per face incidence
+};
+bool build_compact(const MeshTopo& m, const CsrTopo& t, CompactTopo& out);
+
 // Grid detection: true when the mesh is Cloth::new's rows x cols grid with
 // exactly its binding struts after the triangle struts, and the strut ids
 // around every vertex ascend in the order the grid kernel sums them.

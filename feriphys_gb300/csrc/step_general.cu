@@ -18,6 +18,20 @@
 //   face_off[v]..face_off[v+1]    ->  face_inc[e] = face<<2 | corner
 //   face_vtx[f]                   =   {v0, v1, v2, 0}
 // State: pos[v] = {x, y, z, mass}, vel[v] = {vx, vy, vz, pinned ? 1 : 0}.
+//
+// The compact forms (FORM 1 and 2; built by mesh_build.cpp's build_compact)
+// carry the same lists in fewer bytes, which is what bounds this kernel's
+// DRAM traffic: one word per strut incidence (the other vertex as an offset
+// from v, the role, and the strut's rank among its first vertex's struts;
+// 32 bits in form 1, 16 in form 2 when every offset and rank is small), the
+// strut constants as three float arrays in owner order (struts grouped by
+// first vertex, ascending id within a group: v's role-0 incidences take v's
+// group in order, a role-1 incidence takes entry `rank` of its other
+// vertex's group), and one 16-bit word per face incidence (the corner, and
+// where the face's other two vertices sit in v's strut list): 2 or 4 bytes
+// plus 12 / 2 per strut incidence and 2 per face incidence, instead of
+// 8 + 16 and 4 + 16.  The terms and their order are the same, so are the
+// bits.
 #include "kernels.h"
 #include "physics.cuh"
 
@@ -25,39 +39,89 @@ namespace fgb {
 
 namespace {
 
+// One strut term and one face term, added to F in the reference's order.
 template <class T>
+__device__ __forceinline__ void add_strut(V3<T>& F, V3<T> P, V3<T> V, V3<T> Po, V3<T> Vo, int role, float k,
+                                          float cd, float L) {
+  V3<T> sf, df;
+  if (role == 0) {
+    strut_forces<T>(P, Po, V, Vo, T(k), T(cd), T(L), sf, df);
+    F = F + sf;
+    F = F + df;
+  } else {
+    strut_forces<T>(Po, P, Vo, V, T(k), T(cd), T(L), sf, df);
+    F = F + (T(-1) * sf);
+    F = F + (T(-1) * df);
+  }
+}
+template <class T>
+__device__ __forceinline__ void add_face(V3<T>& F, int i0, int i1, int i2, int corner,
+                                         const Vec4<T>* __restrict__ pos, const Vec4<T>* __restrict__ vel,
+                                         V3<T> wind, const StepConsts& c) {
+  const V3<T> x0 = xyz<T>(pos[i0]), x1 = xyz<T>(pos[i1]), x2 = xyz<T>(pos[i2]);
+  const V3<T> v0 = xyz<T>(vel[i0]), v1 = xyz<T>(vel[i1]), v2 = xyz<T>(vel[i2]);
+  const V3<T> total = face_total_force<T>(x0, x1, x2, v0, v1, v2, wind, T(c.neg_drag), T(c.neg_lift));
+  const T w = face_corner_weight<T>(x0, x1, x2, corner);
+  F = F + w * total;
+}
+
+// A strut word of form 1 (32 bits) or 2 (16 bits; a role-0 word has no rank
+// and a 15-bit offset): other-vertex offset, rank, role.
+template <int FORM>
+__device__ __forceinline__ void strut_word(const GeneralTopo& t, int e, int& off, int& rank, int& role) {
+  if (FORM == 2) {
+    const uint32_t w = __ldg(t.strut_word16 + e);
+    role = int(w & 1u);
+    off = int(int16_t(uint16_t(w))) >> (role ? 4 : 1);
+    rank = int((w >> 1) & 7u);  // meaningful for role 1 only
+  } else {
+    const uint32_t w = __ldg(t.strut_word + e);
+    off = int(w) >> 6;
+    rank = int((w >> 1) & 31u);
+    role = int(w & 1u);
+  }
+}
+
+template <class T, int FORM>
 __device__ __forceinline__ V3<T> gather_forces(int v, V3<T> P, V3<T> V, V3<T> F, const Vec4<T>* __restrict__ pos,
                                                const Vec4<T>* __restrict__ vel, const GeneralTopo& t,
                                                const StepConsts& c) {
   const int s_beg = t.strut_off[v], s_end = t.strut_off[v + 1];
+  const V3<T> wind{T(c.wind[0]), T(c.wind[1]), T(c.wind[2])};
+  if (FORM != 0) {
+    int own = t.own_off[v];  // owner position of v's next role-0 strut
+    for (int e = s_beg; e < s_end; ++e) {
+      int off, rank, role;
+      strut_word<FORM>(t, e, off, rank, role);
+      const int o = v + off;
+      const int i = role ? __ldg(t.own_off + o) + rank : own++;
+      add_strut<T>(F, P, V, xyz<T>(pos[o]), xyz<T>(vel[o]), role, __ldg(t.sk + i), __ldg(t.sc + i),
+                   __ldg(t.sl + i));
+    }
+    const int f_beg = t.face_off[v], f_end = t.face_off[v + 1];
+    for (int e = f_beg; e < f_end; ++e) {
+      const uint32_t h = __ldg(t.face_word + e);
+      const int corner = int(h & 3u);
+      int o1, o2, rk, rl;
+      strut_word<FORM>(t, s_beg + int((h >> 2) & 127u), o1, rk, rl);
+      strut_word<FORM>(t, s_beg + int(h >> 9), o2, rk, rl);
+      const int u1 = v + o1, u2 = v + o2;
+      const int i0 = corner == 0 ? v : u1, i1 = corner == 0 ? u1 : (corner == 1 ? v : u2),
+                i2 = corner == 2 ? v : u2;
+      add_face<T>(F, i0, i1, i2, corner, pos, vel, wind, c);
+    }
+    return F;
+  }
   for (int e = s_beg; e < s_end; ++e) {
     const int2 inc = t.strut_inc[e];
-    const int o = inc.x;
-    const int role = inc.y & 1;
     const float4 kcl = t.strut_kcl[inc.y >> 1];
-    const V3<T> Po = xyz<T>(pos[o]);
-    const V3<T> Vo = xyz<T>(vel[o]);
-    V3<T> sf, df;
-    if (role == 0) {
-      strut_forces<T>(P, Po, V, Vo, T(kcl.x), T(kcl.y), T(kcl.z), sf, df);
-      F = F + sf;
-      F = F + df;
-    } else {
-      strut_forces<T>(Po, P, Vo, V, T(kcl.x), T(kcl.y), T(kcl.z), sf, df);
-      F = F + (T(-1) * sf);
-      F = F + (T(-1) * df);
-    }
+    add_strut<T>(F, P, V, xyz<T>(pos[inc.x]), xyz<T>(vel[inc.x]), inc.y & 1, kcl.x, kcl.y, kcl.z);
   }
-  const V3<T> wind{T(c.wind[0]), T(c.wind[1]), T(c.wind[2])};
   const int f_beg = t.face_off[v], f_end = t.face_off[v + 1];
   for (int e = f_beg; e < f_end; ++e) {
     const int fc = t.face_inc[e];
     const int4 fv = t.face_vtx[fc >> 2];
-    const V3<T> x0 = xyz<T>(pos[fv.x]), x1 = xyz<T>(pos[fv.y]), x2 = xyz<T>(pos[fv.z]);
-    const V3<T> v0 = xyz<T>(vel[fv.x]), v1 = xyz<T>(vel[fv.y]), v2 = xyz<T>(vel[fv.z]);
-    const V3<T> total = face_total_force<T>(x0, x1, x2, v0, v1, v2, wind, T(c.neg_drag), T(c.neg_lift));
-    const T w = face_corner_weight<T>(x0, x1, x2, fc & 3);
-    F = F + w * total;
+    add_face<T>(F, fv.x, fv.y, fv.z, fc & 3, pos, vel, wind, c);
   }
   return F;
 }
@@ -68,7 +132,7 @@ __device__ __forceinline__ void flag_nonfinite(bool bad, unsigned* flags) {
 
 // Fused Simulation::step for one mesh (accumulate -> integrate -> collide ->
 // pin restore -> clear), one thread per vertex.
-template <class T>
+template <class T, int FORM>
 __global__ void __launch_bounds__(256) k_step_general(int n, const Vec4<T>* __restrict__ pos,
                                                       const Vec4<T>* __restrict__ vel,
                                                       const Vec4<T>* __restrict__ force_in,
@@ -92,7 +156,7 @@ __global__ void __launch_bounds__(256) k_step_general(int n, const Vec4<T>* __re
   } else {
     F = V3<T>{T(c.force0[0]), T(c.force0[1]), T(c.force0[2])};
   }
-  F = gather_forces<T>(v, P, V, F, pos, vel, t, c);
+  F = gather_forces<T, FORM>(v, P, V, F, pos, vel, t, c);
   V3<T> np, nv, nF;
   integrate_point<T>(c.integration, T(c.dt), P, V, F, m, np, nv, nF);
   collide_point<T>(static_cast<const ObsFace*>(c.obstacle_faces), c.n_obstacle_faces, P, V, F, m, np, nv, c);
@@ -102,7 +166,7 @@ __global__ void __launch_bounds__(256) k_step_general(int n, const Vec4<T>* __re
 }
 
 // accumulate_forces: force[v] = force[v] + gravity + struts + faces; pins -> 0.
-template <class T>
+template <class T, int FORM>
 __global__ void __launch_bounds__(256) k_accumulate(int n, const Vec4<T>* __restrict__ pos,
                                                     const Vec4<T>* __restrict__ vel, Vec4<T>* __restrict__ force,
                                                     GeneralTopo t, StepConsts c) {
@@ -111,7 +175,7 @@ __global__ void __launch_bounds__(256) k_accumulate(int n, const Vec4<T>* __rest
   const Vec4<T> V4 = vel[v];
   const V3<T> g{T(c.force0[0]), T(c.force0[1]), T(c.force0[2])};
   V3<T> F = xyz<T>(force[v]) + g;
-  F = gather_forces<T>(v, xyz<T>(pos[v]), xyz<T>(V4), F, pos, vel, t, c);
+  F = gather_forces<T, FORM>(v, xyz<T>(pos[v]), xyz<T>(V4), F, pos, vel, t, c);
   if (V4.w != T(0)) F = V3<T>{T(0), T(0), T(0)};
   force[v] = make4<T>(F, T(0));
 }
@@ -166,9 +230,10 @@ template <class T>
 cudaError_t launch_step_general(int n, const void* pos, const void* vel, const void* force_in, void* pos_out,
                                 void* vel_out, const GeneralTopo& t, const StepConsts& c, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_step_general<T><<<blocks_for(n, 256), 256, 0, s>>>(
-      n, static_cast<const Vec4<T>*>(pos), static_cast<const Vec4<T>*>(vel), static_cast<const Vec4<T>*>(force_in),
-      static_cast<Vec4<T>*>(pos_out), static_cast<Vec4<T>*>(vel_out), t, c);
+  auto k = t.form == 2 ? k_step_general<T, 2> : (t.form == 1 ? k_step_general<T, 1> : k_step_general<T, 0>);
+  k<<<blocks_for(n, 256), 256, 0, s>>>(n, static_cast<const Vec4<T>*>(pos), static_cast<const Vec4<T>*>(vel),
+                                       static_cast<const Vec4<T>*>(force_in), static_cast<Vec4<T>*>(pos_out),
+                                       static_cast<Vec4<T>*>(vel_out), t, c);
   return cudaGetLastError();
 }
 
@@ -176,9 +241,9 @@ template <class T>
 cudaError_t launch_accumulate(int n, const void* pos, const void* vel, void* force, const GeneralTopo& t,
                               const StepConsts& c, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_accumulate<T><<<blocks_for(n, 256), 256, 0, s>>>(n, static_cast<const Vec4<T>*>(pos),
-                                                     static_cast<const Vec4<T>*>(vel), static_cast<Vec4<T>*>(force),
-                                                     t, c);
+  auto k = t.form == 2 ? k_accumulate<T, 2> : (t.form == 1 ? k_accumulate<T, 1> : k_accumulate<T, 0>);
+  k<<<blocks_for(n, 256), 256, 0, s>>>(n, static_cast<const Vec4<T>*>(pos), static_cast<const Vec4<T>*>(vel),
+                                       static_cast<Vec4<T>*>(force), t, c);
   return cudaGetLastError();
 }
 

@@ -153,16 +153,23 @@ struct Interior {
 // Strut of the compact form: unit vector u and the spring/damper scalars
 // s1 = k(|d| - L), s2 = c (dv . u); the forces are s1*u and s2*u, which a
 // gathering thread forms itself (the same products, so the same bits).
-__device__ __forceinline__ void strut_compact(const float4* __restrict__ s_pos, const float4* __restrict__ s_vel,
-                                              int ia, int ib, float k, float cd, float L, float4* __restrict__ su,
-                                              float* __restrict__ s2) {
-  const V3<float> d = xyz<float>(s_pos[ib]) - xyz<float>(s_pos[ia]);
+__device__ __forceinline__ void strut_terms(float4 pa, float4 pb, float4 va, float4 vb, float k, float cd, float L,
+                                            float4& su, float& s2) {
+  const V3<float> d = xyz<float>(pb) - xyz<float>(pa);
   const float mag = magnitude(d);
   const V3<float> u = d * rcp_of_root(mag);  // 1 / mag, the IEEE bits
   const float s1 = k * (mag - L);
-  const float sd = cd * dot(xyz<float>(s_vel[ib]) - xyz<float>(s_vel[ia]), u);
-  *su = make_float4(u.x, u.y, u.z, s1);
-  *s2 = sd;
+  s2 = cd * dot(xyz<float>(vb) - xyz<float>(va), u);
+  su = make_float4(u.x, u.y, u.z, s1);
+}
+__device__ __forceinline__ void strut_compact(const float4* __restrict__ s_pos, const float4* __restrict__ s_vel,
+                                              int ia, int ib, float k, float cd, float L, float4* __restrict__ su,
+                                              float* __restrict__ s2) {
+  float4 u;
+  float d;
+  strut_terms(s_pos[ia], s_pos[ib], s_vel[ia], s_vel[ib], k, cd, L, u, d);
+  *su = u;
+  *s2 = d;
 }
 
 __device__ __forceinline__ void add_compact(V3<float>& F, float4 su, float s2, int role) {
@@ -192,17 +199,6 @@ __device__ __forceinline__ void quad_to(const float4* __restrict__ s_pos, const 
   *qa = a;
   *qb = b;
   *qw = make_float4(wa.x, wa.y, wb.x, wb.y);
-}
-
-__device__ __forceinline__ void add_pair(V3<float>& F, const float4* __restrict__ pair, int role) {
-  const V3<float> sf = xyz<float>(pair[0]), df = xyz<float>(pair[1]);
-  if (role == 0) {
-    F = F + sf;
-    F = F + df;
-  } else {
-    F = F + (-1.0f * sf);
-    F = F + (-1.0f * df);
-  }
 }
 
 // One CTA = a TW x TH tile: TW*TH "main" threads (one per vertex) plus
@@ -381,11 +377,32 @@ __device__ __forceinline__ void tile_step(int bx, int by, int R, int C, const fl
     strut_compact(s_pos, s_vel, ia, ib, k, cd, L, s_su + kind * NO + o(rr, ccl), s_s2 + kind * NO + o(rr, ccl));
   };
   if (tid < NMAIN) {
-    if (has(KH, lr, lc)) put(KH, lr, lc, q0.x, q0.y, q0.z);
-    if (has(KV, lr, lc)) put(KV, lr, lc, q0.w, q1.x, q1.y);
-    if (has(KS, lr, lc)) put(KS, lr, lc, q1.z, q1.w, q2.x);
-    if (has(KBH, lr, lc)) put(KBH, lr, lc, q2.y, q2.z, q2.w);
-    if (has(KBV, lr, lc)) put(KBV, lr, lc, q3.x, q3.y, q3.z);
+    // the five struts owned by this vertex: first the five strut vectors and
+    // their lengths (independent chains the compiler can interleave), then
+    // each strut's unit vector and scalars, stored where the strut exists
+    // (every slot read lies inside the staged tile; a slot outside the cloth
+    // is never stored)
+    const int i = e(lr, lc);
+    const int ia[5] = {i, i, i + 1, i, i}, ib[5] = {i + 1, i + EW, i + EW, i + 2, i + 2 * EW};
+    const float kk[5] = {q0.x, q0.w, q1.z, q2.y, q3.x}, cc5[5] = {q0.y, q1.x, q1.w, q2.z, q3.y},
+                LL[5] = {q0.z, q1.y, q2.x, q2.w, q3.z};
+    V3<float> d[5];
+    float mag[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) d[j] = xyz<float>(s_pos[ib[j]]) - xyz<float>(s_pos[ia[j]]);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) mag[j] = magnitude(d[j]);
+    const int oi = o(lr, lc);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const V3<float> u = d[j] * rcp_of_root(mag[j]);
+      const float s1 = kk[j] * (mag[j] - LL[j]);
+      const float s2 = cc5[j] * dot(xyz<float>(s_vel[ib[j]]) - xyz<float>(s_vel[ia[j]]), u);
+      if (has(j, lr, lc)) {  // kinds KH, KV, KS, KBH, KBV = 0..4
+        s_su[j * NO + oi] = make_float4(u.x, u.y, u.z, s1);
+        s_s2[j * NO + oi] = s2;
+      }
+    }
   } else {
 #pragma unroll
     for (int j = 0; j < 3; ++j)

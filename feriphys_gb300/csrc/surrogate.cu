@@ -534,6 +534,22 @@ __global__ void __launch_bounds__(128, 1)
 
 // ---- training: fused forward + backward ------------------------------------
 
+// Layout of a CTA's gradient partials: the parameter order, except that the
+// W1 and W2 blocks are stored column by column (entry (o, i) at i * 128 + o),
+// so that the 32 threads of a warp, which hold 32 consecutive rows o of one
+// column i in tensor memory, write 128 consecutive bytes.  The reduction
+// kernels walk the partials in this order and map back.
+__device__ __forceinline__ int partial_of_param(int p) {
+  if (p < kOffB1) return kOffW1 + ((p - kOffW1) % kIn) * kHid + (p - kOffW1) / kIn;
+  if (p >= kOffW2 && p < kOffB2) return kOffW2 + ((p - kOffW2) % kHid) * kHid + (p - kOffW2) / kHid;
+  return p;
+}
+__device__ __forceinline__ int param_of_partial(int q) {
+  if (q < kOffB1) return kOffW1 + ((q - kOffW1) % kHid) * kIn + (q - kOffW1) / kHid;
+  if (q >= kOffW2 && q < kOffB2) return kOffW2 + ((q - kOffW2) % kHid) * kHid + (q - kOffW2) / kHid;
+  return q;
+}
+
 constexpr int kTrX = kBlobSmem;            // 128 x 64
 constexpr int kTrH1 = kTrX + 16384;        // 128 x 128
 constexpr int kTrH2 = kTrH1 + 32768;
@@ -720,12 +736,12 @@ __global__ void __launch_bounds__(kTrThreads, 1)
 #pragma unroll 1
     for (int cb = half * (kIn / 2); cb < (half + 1) * (kIn / 2); cb += 32) {
       tc::tmem_ld32(tmem + kCW1 + lane_off + cb, v);
-      for (int j = 0; j < 32; ++j) P[kOffW1 + row * kIn + cb + j] = v[j];
+      for (int j = 0; j < 32; ++j) P[partial_of_param(kOffW1 + row * kIn + cb + j)] = v[j];
     }
 #pragma unroll 1
     for (int cb = c0; cb < c1; cb += 32) {
       tc::tmem_ld32(tmem + kCW2 + lane_off + cb, v);
-      for (int j = 0; j < 32; ++j) P[kOffW2 + row * kHid + cb + j] = v[j];
+      for (int j = 0; j < 32; ++j) P[partial_of_param(kOffW2 + row * kHid + cb + j)] = v[j];
     }
     if (half == 0) {  // warp-uniform
       float u[16];
@@ -784,26 +800,31 @@ __device__ __forceinline__ float loss_sum(const float* partials, int ctas) {
   return s;
 }
 
-__device__ __forceinline__ float grad_sum(const float* partials, int ctas, int p) {
+// the gradient of parameter p = param_of_partial(q), summed over the CTAs in
+// CTA order (the threads of a block read consecutive partials q)
+__device__ __forceinline__ float grad_sum(const float* partials, int ctas, int q, int p) {
   float g = 0.0f;
-  for (int c = 0; c < ctas; ++c) g += partials[size_t(c) * kPartialStride + p];
+  for (int c = 0; c < ctas; ++c) g += partials[size_t(c) * kPartialStride + q];
   return param_used(p) ? g : 0.0f;
 }
 
 __global__ void k_reduce_grad(const float* __restrict__ partials, int ctas, float inv_count, float* __restrict__ grad,
                               float* __restrict__ loss_out) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p == 0 && loss_out) loss_out[0] = loss_sum(partials, ctas) * inv_count;
-  if (p < kNumParams) grad[p] = grad_sum(partials, ctas, p);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q == 0 && loss_out) loss_out[0] = loss_sum(partials, ctas) * inv_count;
+  if (q >= kNumParams) return;
+  const int p = param_of_partial(q);
+  grad[p] = grad_sum(partials, ctas, q, p);
 }
 
 __global__ void k_adam(const float* __restrict__ partials, int ctas, float* __restrict__ master, float* __restrict__ m,
                        float* __restrict__ v, float lr, float beta1, float beta2, float eps, float c1, float c2,
                        unsigned char* __restrict__ blob, float* __restrict__ loss_out, float inv_count) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p == 0 && loss_out) loss_out[0] = loss_sum(partials, ctas) * inv_count;
-  if (p >= kNumParams) return;
-  const float g = grad_sum(partials, ctas, p);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q == 0 && loss_out) loss_out[0] = loss_sum(partials, ctas) * inv_count;
+  if (q >= kNumParams) return;
+  const int p = param_of_partial(q);
+  const float g = grad_sum(partials, ctas, q, p);
   const float mm = beta1 * m[p] + (1.0f - beta1) * g;
   const float vv = beta2 * v[p] + (1.0f - beta2) * (g * g);
   m[p] = mm;

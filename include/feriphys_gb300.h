@@ -163,7 +163,10 @@ int fgb_mesh_export_indices(fgb_mesh* m, void* device_out, void* stream);
  * is a Cloth::new grid, else the general gather), 1 = general gather,
  * 2 = grid kernel (fails with FGB_ESTATE if the mesh is not a grid),
  * 3 = the grid kernel's untiled form (one thread per vertex, no shared
- * memory; a cross-check of the tiled one).  All give identical results. */
+ * memory; a cross-check of the tiled one), 4 = the general gather over its
+ * plain incidence lists (a cross-check of the compact lists path 1 reads
+ * when the mesh fits them).  All give identical results; fgb_mesh_get_path
+ * reports 4 as 1. */
 int fgb_mesh_set_path(fgb_mesh* m, int path);
 
 /* Which path the next step uses (1 general, 2 grid); decided on the host. */

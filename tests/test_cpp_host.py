@@ -53,3 +53,26 @@ def test_sim_rejects_meshes_of_different_devices(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+def test_compact_incidence_lists_decode_to_the_csr(tmp_path):
+    """The general gather's compact lists (mesh_build.h: CompactTopo) decode
+    to the plain CSR lists on cloth grids and a random triangle soup, and a
+    mesh beyond their limits is refused (tests/cpp/compact_topo.cpp calls the
+    library's internal builders; no GPU)."""
+    import feriphys_gb300
+
+    lib = feriphys_gb300.library_path()
+    feriphys_gb300._lib()
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    exe = str(tmp_path / "compact_topo")
+    libdir = os.path.dirname(lib)
+    cmd = [gxx, "-std=c++17", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-I",
+           os.path.join(ROOT, "feriphys_gb300", "csrc"), os.path.join(ROOT, "tests", "cpp", "compact_topo.cpp"),
+           "-o", exe, "-L", libdir, "-lferiphys_gb300", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr

@@ -94,14 +94,15 @@ def test_c0_aero_off_bit_exact(fgb, orc, W, path):
 
 @pytest.mark.parametrize("rows,cols", [(24, 24), (2, 2), (3, 5), (37, 29), (9, 70), (70, 95), (41, 63), (5, 33)])
 def test_step_forms_bit_identical(fgb, W, rows, cols):
-    """General gather (1), tiled grid (2) and untiled grid (3) kernels agree
-    bit for bit, including cloths that do not fill whole 32x8 tiles."""
+    """General gather (1), tiled grid (2), untiled grid (3) kernels and the
+    general gather over its plain incidence lists (4) agree bit for bit,
+    including cloths that do not fill whole 32x8 tiles."""
     s = 1.0 / 31
     lt, ls, lb = s, s * 2 ** 0.5, 2 * s
     args = (rows, cols, s, (0.0, 0.0, 0.0), 0.01, 500 * lt, 0.5 * lt, 250 * ls, 0.5 * ls, 50 * lb, 0.5 * lb)
     pins = [rows * cols - 1]
     out = []
-    for path in (1, 2, 3):
+    for path in (1, 2, 3, 4):
         mesh = fgb.Cloth.new(*args, pins).mesh
         mesh.set_path(path)
         sim = fgb.Simulation.new([mesh], [fgb.CollidableMesh.new(*W.plane(-0.3))])
@@ -219,6 +220,48 @@ def test_general_mesh(fgb, orc, W, integration):
                                    c["drag_coefficient"], c["coefficient_of_restitution"],
                                    c["coefficient_of_friction"]))
     compare_steps((gs, g, None), (os_, o, None), 100, PER_STEP_TOL)
+
+
+@pytest.mark.parametrize("bits,spread", [(32, False), (64, False), (32, True)])
+def test_general_lists_bit_identical(fgb, W, bits, spread):
+    """The general gather over its compact incidence lists (path 1) and over
+    the plain CSR lists (path 4) give the same bits, in f32 and f64, for the
+    fused step and for accumulate_forces, on a random mesh with (k, c)
+    overrides and extra struts.  spread: the mesh's vertices scattered over
+    6000 ids (the rest free points without struts), so that neighbour offsets
+    exceed the 16-bit strut words and the 32-bit form is read."""
+    rng = np.random.default_rng(5)
+    pos, idx = _random_mesh(rng)
+    if spread:
+        ids = rng.permutation(6000)[:len(pos)].astype(np.uint32)
+        big = rng.uniform(-1.0, 1.0, (6000, 3)).astype(np.float32)
+        big[ids] = pos
+        pos, idx = big, ids[idx]
+    pairs = idx[:12].reshape(-1, 2)
+    kc = np.stack([rng.uniform(8.0, 16.0, len(pairs)), rng.uniform(0.01, 0.03, len(pairs))], 1).astype(np.float32)
+    cfg = fgb.Config.make(**W.cloth_config(1.0 / 1200.0))
+    out = []
+    for path in (1, 4):
+        m = fgb.SpringyMesh.new(pos, idx, 0.81, 12.0, 0.02, (pairs, kc))
+        m.add_strut((int(idx[0]), int(idx[20])), 3.0, 0.01)
+        m.add_strut((int(idx[40]), int(idx[3])), 3.0, 0.01)
+        m.add_pin(int(idx[80]))
+        m.set_path(path)
+        m.set_precision(bits)
+        sim = fgb.Simulation.new([m], [fgb.CollidableMesh.new(*W.plane(-0.05, 1.0))])
+        sim.set_config(cfg)
+        p = m.get_points()
+        p[:, 4:7] = rng.normal(0, 0.3, (len(p), 3)) if path == 1 else out[0][2]
+        m.set_points(p)
+        vel = p[:, 4:7].copy()
+        sim.step(50)
+        got = m.get_points_f64() if bits == 64 else m.get_points()
+        m.accumulate_forces(cfg)
+        forces = m.get_points_f64() if bits == 64 else m.get_points()
+        assert m.get_path() == 1
+        out.append((got.tobytes(), forces.tobytes(), vel))
+    assert out[0][0] == out[1][0]
+    assert out[0][1] == out[1][1]
 
 
 def test_phase_hooks_match_oracle(fgb, orc, W):
