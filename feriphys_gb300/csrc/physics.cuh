@@ -129,6 +129,19 @@ __device__ __forceinline__ void integrate_point(int integration, T h, V3<T> p, V
   }
 }
 
+// x unchanged, opaque to the compiler: an expression of it cannot be moved
+// out of the branch it sits in.  The crossing test's divisions by dt depend
+// only on the point, so without this the compiler hoists them out of the
+// candidate loop and every point pays three IEEE divisions, crossing or not.
+__device__ __forceinline__ float opaque(float x) {
+  asm volatile("" : "+f"(x));
+  return x;
+}
+__device__ __forceinline__ double opaque(double x) {
+  asm volatile("" : "+d"(x));
+  return x;
+}
+
 // The crossing test of one face (collidable_mesh.rs:107-145): signs of the
 // plane distances differ and the projected point lies inside the triangle.
 // The triangle's other vertices are only loaded once the plane is crossed.
@@ -141,7 +154,7 @@ __device__ __forceinline__ bool face_hit(const ObsFace* __restrict__ Fp, V3<T> o
   d_old = dot(op - v0, n);
   d_new = dot(np - v0, n);
   if (signbit(d_old) == signbit(d_new)) return false;
-  const V3<T> ovel = (np - op) / dtd;
+  const V3<T> ovel = (np - op) / opaque(dtd);
   const T fr = d_old / (d_old - d_new);
   const V3<T> cp = op + (dtd * fr) * ovel;
   const float4 fv1 = Fp->v1, fv2 = Fp->v2;
