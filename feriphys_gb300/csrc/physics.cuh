@@ -208,9 +208,12 @@ __device__ __forceinline__ bool collide_point_all(const ObsFace* __restrict__ fa
 }
 
 // Margin of the query box: the computed crossing point can leave the
-// segment's box by a few ulps of the step and of the coordinates.
+// segment's box by a few ulps of the step and of the coordinates.  The
+// margin 1e-5 |a - b| + 1e-5 max(|a|, |b|) covers that many times over;
+// since |a - b| <= 2 max(|a|, |b|), 3.0001e-5 max(|a|, |b|) covers it too,
+// in fewer operations (a larger box only adds candidates).
 __device__ __forceinline__ float query_slack(float a, float b) {
-  return 1e-5f * fabsf(a - b) + 1e-5f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f;
+  return 3.0001e-5f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f;
 }
 
 template <class T>
@@ -270,8 +273,10 @@ __device__ __forceinline__ bool collide_point(const ObsFace* __restrict__ faces,
     } else {
       const ObsGrid3& g = A.grids[k];
       bool all = false;
-      if (g.n[0] > 0 && hi[0] >= g.lo[0] && lo[0] <= g.hi[0] && hi[1] >= g.lo[1] && lo[1] <= g.hi[1] &&
-          hi[2] >= g.lo[2] && lo[2] <= g.hi[2]) {
+      const bool meets = g.n[0] > 0 && hi[0] >= g.lo[0] && lo[0] <= g.hi[0] && hi[1] >= g.lo[1] &&
+                         lo[1] <= g.hi[1] && hi[2] >= g.lo[2] && lo[2] <= g.hi[2];
+      if (!meets && g.n_always == 0) continue;  // no face of this obstacle can be hit
+      if (meets) {
         int idx[3];
         bool fits = true;
 #pragma unroll
