@@ -5,8 +5,9 @@
 // Vector3::angle(a, b) = atan2(|a x b|, a . b).  The library is compiled with
 // -fmad=false so no a*b+c is fused, and '/' and sqrt are the IEEE-rounded
 // operations; with the same operation order the results are bit-identical to
-// the reference's f32 arithmetic except where a libm function (atan2f) is
-// involved (angle.cuh).
+// the reference's f32 arithmetic except in the faces' corner angles: the
+// atan2 is the library's own (angle.cuh), and the three corners share one
+// cross-product magnitude (physics.cuh: face_corner_weight).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -52,8 +53,9 @@ template <class T> __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
 }
 __device__ __forceinline__ float sq_root(float v) { return sqrtf(v); }
 __device__ __forceinline__ double sq_root(double v) { return sqrt(v); }
-// atan2(y, x) for y >= 0 (the angle between two vectors, see vangle): the
-// f32 form is angle.cuh's, the f64 form (the FP64 rerun) libm's.
+// atan2(y, x) for y >= 0 (the angle between two vectors: cgmath's
+// Vector3::angle(a, b) = atan2(|a x b|, a . b)): the f32 form is angle.cuh's,
+// the f64 form (the FP64 rerun) libm's.
 #if defined(__CUDACC__)
 __device__ __forceinline__ float angle_of(float y, float x) { return angle_pos(y, x); }
 __device__ __forceinline__ double angle_of(double y, double x) { return atan2(y, x); }
@@ -68,7 +70,6 @@ __device__ __forceinline__ float min_num(float a, float b) { return fminf(a, b);
 __device__ __forceinline__ double min_num(double a, double b) { return fmin(a, b); }
 template <class T> __device__ __forceinline__ T magnitude(V3<T> v) { return sq_root(dot(v, v)); }
 template <class T> __device__ __forceinline__ V3<T> normalize(V3<T> v) { return v * inv_magnitude(magnitude(v)); }
-template <class T> __device__ __forceinline__ T vangle(V3<T> a, V3<T> b) { return angle_of(magnitude(cross(a, b)), dot(a, b)); }
 template <class T> __device__ __forceinline__ bool is_zero(V3<T> v) { return v.x == T(0) && v.y == T(0) && v.z == T(0); }
 template <class T> __device__ __forceinline__ bool finite3(V3<T> v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
 

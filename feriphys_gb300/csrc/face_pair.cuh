@@ -62,9 +62,10 @@ static __device__ __noinline__ f2 div2_ieee_cold(f2 a, float b) {
 
 // drag + lift (D) and the three corner weights angle_k / PI of two faces
 // (springy_mesh.rs:629-654, 134-172), lane 0 and lane 1.  The corner angles
-// reuse exact identities: |(x2-x0) x (x1-x0)| is bitwise |(x1-x0) x (x2-x0)|,
-// and x0-x1 = -(x1-x0), x1-x2 = -(x2-x1) exactly.  The divisions by 3 and pi
-// take one guard per group of three per face (div_const_try).
+// take y = |(x1-x0) x (x2-x0)| at all three corners, as face_corner_weight
+// does, and their dot products through exact identities: x0-x1 = -(x1-x0)
+// and x1-x2 = -(x2-x1) exactly.  The divisions by 3 and pi take one guard
+// per group of three per face (div_const_try).
 __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, V3x2 v1, V3x2 v2, V3x2 wind,
                                             float neg_cd, float neg_lift, float one_rt, float4& DwA, float2& wA,
                                             float4& DwB, float2& wB) {
@@ -87,8 +88,8 @@ __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, 
   const V3x2 lift = scale3(mul2(dup2(neg_lift), eff), V3x2{mul2(rv.x, m2), mul2(rv.y, m2), mul2(rv.z, m2)});
   const V3x2 D{add_p2(lift.x, drag.x, one), add_p2(lift.y, drag.y, one), add_p2(lift.z, drag.z, one)};
   const f2 a0 = angle_pos2(mag, dot3(e2, e1, one), one);
-  const f2 a1 = angle_pos2(magnitude3(cross3(e1, e3, one), one), neg2(dot3(e1, e3, one)), one);
-  const f2 a2 = angle_pos2(magnitude3(cross3(e3, e2, one), one), dot3(e3, e2, one), one);
+  const f2 a1 = angle_pos2(mag, neg2(dot3(e1, e3, one)), one);
+  const f2 a2 = angle_pos2(mag, dot3(e3, e2, one), one);
   bool okw = true;
   f2 w0 = div_const2(a0, kPiF32, kRcpPi, okw), w1 = div_const2(a1, kPiF32, kRcpPi, okw),
      w2 = div_const2(a2, kPiF32, kRcpPi, okw);

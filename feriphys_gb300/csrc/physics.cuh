@@ -41,14 +41,21 @@ __device__ __forceinline__ V3<T> face_total_force(V3<T> x0, V3<T> x1, V3<T> x2, 
   return drag + lift;
 }
 
-// Vertex angle of corner k over PI (springy_mesh.rs:134-172, 647-649).
+// Vertex angle of corner k over PI (springy_mesh.rs:134-172, 647-649).  The
+// reference takes each corner's angle as atan2(|a x b|, a . b) of that
+// corner's two edges; |a x b| is twice the face's area at every corner, so
+// all three corners here take the one magnitude |(x1 - x0) x (x2 - x0)| the
+// drag already needs (the reference's per-corner recomputations of it
+// differ from it by rounding only, like the angle's own last bits), and only
+// the dot products are per corner, in the reference's order.
 template <class T>
 __device__ __forceinline__ T face_corner_weight(V3<T> x0, V3<T> x1, V3<T> x2, int k) {
-  T a;
-  if (k == 0) a = vangle(x2 - x0, x1 - x0);
-  else if (k == 1) a = vangle(x0 - x1, x2 - x1);
-  else a = vangle(x1 - x2, x0 - x2);
-  return a / T(kPiF32);
+  const T y = magnitude(cross(x1 - x0, x2 - x0));
+  T x;
+  if (k == 0) x = dot(x2 - x0, x1 - x0);
+  else if (k == 1) x = dot(x0 - x1, x2 - x1);
+  else x = dot(x1 - x2, x0 - x2);
+  return angle_of(y, x) / T(kPiF32);
 }
 
 // F / m componentwise, exactly as IEEE division; the f32 form shares one
