@@ -61,11 +61,11 @@ static __device__ __noinline__ f2 div2_ieee_cold(f2 a, float b) {
 }
 
 // drag + lift (D) and the three corner weights angle_k / PI of two faces
-// (springy_mesh.rs:629-654, 134-172), lane 0 and lane 1.  The corner angles
-// take y = |(x1-x0) x (x2-x0)| at all three corners, as face_corner_weight
-// does, and their dot products through exact identities: x0-x1 = -(x1-x0)
-// and x1-x2 = -(x2-x1) exactly.  The divisions by 3 and pi take one guard
-// per group of three per face (div_const_try).
+// (springy_mesh.rs:629-654, 134-172), lane 0 and lane 1, as
+// face_total_force and face_corner_weight compute them: corners 0 and 1 take
+// y = |(x1-x0) x (x2-x0)| and their dot products (x0-x1 = -(x1-x0) exactly),
+// corner 2 the rest of the unit share.  The divisions by 3 and pi take one
+// guard per group per face (div_const_try).
 __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, V3x2 v1, V3x2 v2, V3x2 wind,
                                             float neg_cd, float neg_lift, float one_rt, float4& DwA, float2& wA,
                                             float4& DwB, float2& wB) {
@@ -89,15 +89,13 @@ __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, 
   const V3x2 D{add_p2(lift.x, drag.x, one), add_p2(lift.y, drag.y, one), add_p2(lift.z, drag.z, one)};
   const f2 a0 = angle_pos2(mag, dot3(e2, e1, one), one);
   const f2 a1 = angle_pos2(mag, neg2(dot3(e1, e3, one)), one);
-  const f2 a2 = angle_pos2(mag, dot3(e3, e2, one), one);
   bool okw = true;
-  f2 w0 = div_const2(a0, kPiF32, kRcpPi, okw), w1 = div_const2(a1, kPiF32, kRcpPi, okw),
-     w2 = div_const2(a2, kPiF32, kRcpPi, okw);
+  f2 w0 = div_const2(a0, kPiF32, kRcpPi, okw), w1 = div_const2(a1, kPiF32, kRcpPi, okw);
   if (!okw) {
     w0 = div2_ieee_cold(a0, kPiF32);
     w1 = div2_ieee_cold(a1, kPiF32);
-    w2 = div2_ieee_cold(a2, kPiF32);
   }
+  const f2 w2 = sub2(sub2(dup2(1.0f), w0), w1);  // (1 - w0) - w1
   const float2 dx = upk(D.x), dy = upk(D.y), dz = upk(D.z), u0 = upk(w0), u1 = upk(w1), u2 = upk(w2);
   DwA = make_float4(dx.x, dy.x, dz.x, u0.x);
   DwB = make_float4(dx.y, dy.y, dz.y, u0.y);

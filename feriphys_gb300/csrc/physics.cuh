@@ -43,19 +43,32 @@ __device__ __forceinline__ V3<T> face_total_force(V3<T> x0, V3<T> x1, V3<T> x2, 
 
 // Vertex angle of corner k over PI (springy_mesh.rs:134-172, 647-649).  The
 // reference takes each corner's angle as atan2(|a x b|, a . b) of that
-// corner's two edges; |a x b| is twice the face's area at every corner, so
-// all three corners here take the one magnitude |(x1 - x0) x (x2 - x0)| the
-// drag already needs (the reference's per-corner recomputations of it
-// differ from it by rounding only, like the angle's own last bits), and only
-// the dot products are per corner, in the reference's order.
+// corner's two edges; the FP64 rerun (T = double) does exactly that.  The f32
+// step saves work the reference repeats: |a x b| is twice the face's area at
+// every corner, so corners 0 and 1 take the one magnitude
+// |(x1 - x0) x (x2 - x0)| the drag already needs, with their own dot products
+// in the reference's order; and the angles sum to pi, so corner 2's share is
+// (1 - w0) - w1.  Both differ from the reference's per-corner recomputation
+// by rounding only (about 1e-7 of the face's force), like the angle's own
+// last bits.
+template <class T>
+__device__ __forceinline__ T corner_share(V3<T> x0, V3<T> x1, V3<T> x2, T y, int k) {
+  const T x = k == 0 ? dot(x2 - x0, x1 - x0) : dot(x0 - x1, x2 - x1);
+  return angle_of(y, x) / T(kPiF32);
+}
 template <class T>
 __device__ __forceinline__ T face_corner_weight(V3<T> x0, V3<T> x1, V3<T> x2, int k) {
-  const T y = magnitude(cross(x1 - x0, x2 - x0));
-  T x;
-  if (k == 0) x = dot(x2 - x0, x1 - x0);
-  else if (k == 1) x = dot(x0 - x1, x2 - x1);
-  else x = dot(x1 - x2, x0 - x2);
-  return angle_of(y, x) / T(kPiF32);
+  if constexpr (sizeof(T) == 8) {  // the reference's form
+    V3<T> a, b;
+    if (k == 0) { a = x2 - x0; b = x1 - x0; }
+    else if (k == 1) { a = x0 - x1; b = x2 - x1; }
+    else { a = x1 - x2; b = x0 - x2; }
+    return angle_of(magnitude(cross(a, b)), dot(a, b)) / T(kPiF32);
+  } else {
+    const T y = magnitude(cross(x1 - x0, x2 - x0));
+    if (k < 2) return corner_share(x0, x1, x2, y, k);
+    return (T(1) - corner_share(x0, x1, x2, y, 0)) - corner_share(x0, x1, x2, y, 1);
+  }
 }
 
 // F / m componentwise, exactly as IEEE division; the f32 form shares one
