@@ -8,8 +8,9 @@
 // term, then for each incident face in increasing face index its corner
 // share.  The incidence lists here are sorted exactly that way, so each
 // vertex sums the same terms in the same order as the reference and the
-// result is bit-identical (with -fmad=false) except for atan2f's last bit in
-// the face weights.
+// result is bit-identical (with -fmad=false) except in the face weights
+// (physics.cuh: face_corner_weight; in f32 their corner angles differ from
+// the reference's by rounding).
 //
 // Layout (one entry per incidence):
 //   strut_off[v]..strut_off[v+1]  ->  strut_inc[e] = {other vertex, strut<<1 | role}

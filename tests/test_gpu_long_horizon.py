@@ -12,8 +12,8 @@ oracle counts those hits (springy_mesh.rs:423-497 through the first-hit
 search) so the test knows the collision path ran.
 
 Bars: relative position error <= 1e-3 after 1000 steps with the aerodynamic
-terms on (the only difference is atan2f's last bit), and bit-identical
-states over 200 steps with drag and lift off.  The oracle trajectories run in
+terms on (the only differences are the face corner angles' last bits), and
+bit-identical states over 200 steps with drag and lift off.  The oracle trajectories run in
 worker processes (spawned, CUDA-free) while the GPU steps.
 """
 import concurrent.futures as cf

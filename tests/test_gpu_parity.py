@@ -3,8 +3,9 @@
 Error measure: relative position error = max_i |p_gpu_i - p_ref_i| / max_i |p_ref_i|
 (the same for velocities).  Bars: 1e-5 per step against the f32 oracle,
 1e-3 after 1000 steps; bit-identical when the aerodynamic terms are off
-(the only libm call on the path, atan2f, then drops out); the grid-stencil
-and general-gather kernels must agree bit for bit with each other.
+(the f32 step leaves the reference's arithmetic only in the face terms'
+corner angles); the grid-stencil and general-gather kernels must agree bit
+for bit with each other.
 """
 import numpy as np
 import pytest
@@ -73,8 +74,9 @@ def test_c0_per_step(fgb, orc, W, path):
 
 def test_c0_free_trajectory(fgb, orc, W):
     # Without resets the GPU and oracle trajectories separate only through
-    # atan2f's last bit; at the configured dt=1/600 explicit Euler is
-    # unstable, which amplifies that, so the bar here is the long-horizon one.
+    # the corner angles' last bits; at the configured dt=1/600 explicit Euler
+    # is unstable, which amplifies that, so the bar here is the long-horizon
+    # one.
     g, o = both(W.c0(), fgb, orc, W)
     worst = compare_steps(g, o, 100, LONG_TOL, reset=False)
     print("c0 free trajectory: worst relative error over 100 steps %.3g" % worst)
