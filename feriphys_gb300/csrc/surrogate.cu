@@ -279,6 +279,8 @@ __device__ __forceinline__ void store_input_row(unsigned char* X, int lt, const 
 
 // z (TMEM lane = this thread's row, columns [c0, c1)) + bias -> GELU -> bf16
 // row of the 128-wide tile H; with G != null also the GELU slope into G.
+// BIAS = false: the accumulator already holds the bias (bias_to_tmem).
+template <bool BIAS = true>
 __device__ __forceinline__ void epilogue_gelu(uint32_t taddr, const float* __restrict__ bias, unsigned char* H,
                                               unsigned char* G, int lt, int c0 = 0, int c1 = kHid) {
   const f32x2* __restrict__ bias2 = reinterpret_cast<const f32x2*>(bias);
@@ -292,7 +294,8 @@ __device__ __forceinline__ void epilogue_gelu(uint32_t taddr, const float* __res
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int a = 8 * q + 2 * j;
-        const f32x2 x = tc::f2_add(tc::f2_pack(z[a], z[a + 1]), bias2[(cb + a) >> 1]);
+        const f32x2 zz = tc::f2_pack(z[a], z[a + 1]);
+        const f32x2 x = BIAS ? tc::f2_add(zz, bias2[(cb + a) >> 1]) : zz;
         if (G)
           gelu2_slope_bf(x, uh[j], ug[j]);
         else
@@ -330,6 +333,26 @@ __device__ __forceinline__ void epilogue_backward(uint32_t taddr, unsigned char*
   }
 }
 
+// The layer's bias as the initial value of this thread's accumulator row
+// (TMEM lane = its row, columns [c0, c1)): the MMAs then accumulate onto it,
+// so the epilogue has no bias to add.
+__device__ __forceinline__ void bias_to_tmem(uint32_t taddr, const float* __restrict__ bias, int c0, int c1) {
+#pragma unroll 1
+  for (int cb = c0; cb < c1; cb += 32) {
+    float v[32];
+    const float4* b4 = reinterpret_cast<const float4*>(bias + cb);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const float4 q = b4[k];
+      v[4 * k] = q.x;
+      v[4 * k + 1] = q.y;
+      v[4 * k + 2] = q.z;
+      v[4 * k + 3] = q.w;
+    }
+    tc::tmem_st32(taddr + cb, v);
+  }
+}
+
 // The three layers for the tile in `act` (inputs in the 64-wide layout on
 // entry; the hidden activations overwrite it), run by a group of 128 * H
 // threads: thread lt of the group owns row lt % 128 and the hidden columns
@@ -349,27 +372,29 @@ __device__ __forceinline__ bool mlp_tile(unsigned char* act, const unsigned char
   const float* b3 = reinterpret_cast<const float*>(wsm + kBlobB3);
   constexpr uint32_t id_hid = tc::idesc_bf16(128, kHid), id_out = tc::idesc_bf16(128, kOutPad);
 
+  bias_to_tmem(tmem + lane_off, b1, c0, c0 + NC);
   sync_for_mma(bar_id, NT);
   if (lt == 0) {
 #pragma unroll
     for (int s = 0; s < kIn / 16; ++s)
       tc::mma_bf16(tmem, tc::sdesc(a_act + 256 * s, 128, kIn * 16), tc::sdesc(a_w1 + 256 * s, 128, kIn * 16), id_hid,
-                   s > 0);
+                   true);
     tc::mma_commit(bar);
   }
   if (!group_wait(bar, phase, bar_id, fail_flag, NT)) return false;
-  epilogue_gelu(tmem + lane_off, b1, act, nullptr, row, c0, c0 + NC);
+  epilogue_gelu<false>(tmem + lane_off, b1, act, nullptr, row, c0, c0 + NC);
 
+  bias_to_tmem(tmem + lane_off, b2, c0, c0 + NC);
   sync_for_mma(bar_id, NT);
   if (lt == 0) {
 #pragma unroll
     for (int s = 0; s < kHid / 16; ++s)
       tc::mma_bf16(tmem, tc::sdesc(a_act + 256 * s, 128, kHid * 16), tc::sdesc(a_w2 + 256 * s, 128, kHid * 16),
-                   id_hid, s > 0);
+                   id_hid, true);
     tc::mma_commit(bar);
   }
   if (!group_wait(bar, phase, bar_id, fail_flag, NT)) return false;
-  epilogue_gelu(tmem + lane_off, b2, act, nullptr, row, c0, c0 + NC);
+  epilogue_gelu<false>(tmem + lane_off, b2, act, nullptr, row, c0, c0 + NC);
 
   sync_for_mma(bar_id, NT);
   if (lt == 0) {
