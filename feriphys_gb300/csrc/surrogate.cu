@@ -650,28 +650,32 @@ __global__ void __launch_bounds__(kTrThreads, 1)
       tc::bulk_g2s(sX, X + size_t(t) * 16384, 16384, &bar_x);
     }
     const float4 tg = reinterpret_cast<const float4*>(T)[size_t(t) * 128 + row];
+    // the layer biases as the accumulators' starting values, as in inference
+    bias_to_tmem(tmem + kCA + lane_off, b1, c0, c1);
+    bias_to_tmem(tmem + kCB + lane_off, b2, c0, c1);
+    tc::fence_before_sync();
     if (!(ok = group_wait(&bar_x, ph_x, 0, &fail))) break;
     // layer 1: z1 -> cols [0, 128)
     if (lt == 0) {
 #pragma unroll
       for (int s = 0; s < kIn / 16; ++s)
         tc::mma_bf16(tmem + kCA, tc::sdesc(aX + 256 * s, 128, kIn * 16), tc::sdesc(aW1 + 256 * s, 128, kIn * 16),
-                     tc::idesc_bf16(128, kHid), s > 0);
+                     tc::idesc_bf16(128, kHid), true);
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_gelu(tmem + kCA + lane_off, b1, sH1, sG1, row, c0, c1);
+    epilogue_gelu<false>(tmem + kCA + lane_off, b1, sH1, sG1, row, c0, c1);
     sync_for_mma(0);
     // layer 2: z2 -> cols [128, 256)
     if (lt == 0) {
 #pragma unroll
       for (int s = 0; s < kHid / 16; ++s)
         tc::mma_bf16(tmem + kCB, tc::sdesc(aH1 + 256 * s, 128, KM_H), tc::sdesc(aW2 + 256 * s, 128, KM_H),
-                     tc::idesc_bf16(128, kHid), s > 0);
+                     tc::idesc_bf16(128, kHid), true);
       tc::mma_commit(&bar_m);
     }
     if (!(ok = group_wait(&bar_m, ph_m, 0, &fail))) break;
-    epilogue_gelu(tmem + kCB + lane_off, b2, sH2, sG2, row, c0, c1);
+    epilogue_gelu<false>(tmem + kCB + lane_off, b2, sH2, sG2, row, c0, c1);
     sync_for_mma(0);
     // layer 3: y -> cols [0, 16)
     if (lt == 0) {
