@@ -45,37 +45,21 @@ __device__ __forceinline__ f2 rcp_of_root2(f2 x) {
   return pk(y1.x != y1.x ? z.x : y1.x, y1.y != y1.y ? z.y : y1.y);
 }
 
-// a / b for b = 3 or pi in both lanes (div_const_try); ok cleared when a
-// lane needs the IEEE division.
-__device__ __forceinline__ f2 div_const2(f2 a, float b, float y, bool& ok) {
-  const f2 q = mul2(a, dup2(y));
-  const f2 r = fma2(dup2(-b), q, a);
-  const f2 q2 = fma2(r, dup2(y), q);
-  const float2 u = upk(a);
-  ok = ok && div_const_ok(u.x) && div_const_ok(u.y);
-  return q2;
-}
-static __device__ __noinline__ f2 div2_ieee_cold(f2 a, float b) {
-  const float2 u = upk(a);
-  return pk(u.x / b, u.y / b);
-}
-
 // drag + lift (D) and the three corner weights angle_k / PI of two faces
 // (springy_mesh.rs:629-654, 134-172), lane 0 and lane 1, as
 // face_total_force and face_corner_weight compute them: corners 0 and 1 take
 // y = |(x1-x0) x (x2-x0)| and their dot products (x0-x1 = -(x1-x0) exactly),
-// corner 2 the rest of the unit share.  The divisions by 3 and pi take one
-// guard per group per face (div_const_try).
+// corner 2 the rest of the unit share; the mean velocity and the shares by
+// multiplication with RN(1/3) and RN(1/pi).
 __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, V3x2 v1, V3x2 v2, V3x2 wind,
                                             float neg_cd, float neg_lift, float one_rt, float4& DwA, float2& wA,
                                             float4& DwB, float2& wB) {
   const f2 one = dup2(one_rt);
   const V3x2 sum = add3(add3(v0, v1), v2);
-  bool ok = true;
-  V3x2 avg{div_const2(sum.x, 3.0f, kRcp3, ok), div_const2(sum.y, 3.0f, kRcp3, ok),
-           div_const2(sum.z, 3.0f, kRcp3, ok)};
-  if (!ok) avg = V3x2{div2_ieee_cold(sum.x, 3.0f), div2_ieee_cold(sum.y, 3.0f), div2_ieee_cold(sum.z, 3.0f)};
-  const V3x2 rv = sub3(avg, wind);
+  const f2 r3 = dup2(kRcp3);
+  // rv = avg - wind with avg = sum * RN(1/3) kept rounded (add_p2)
+  const V3x2 rv{add_p2(mul2(sum.x, r3), neg2(wind.x), one), add_p2(mul2(sum.y, r3), neg2(wind.y), one),
+                add_p2(mul2(sum.z, r3), neg2(wind.z), one)};
   const V3x2 e1 = sub3(x1, x0), e2 = sub3(x2, x0), e3 = sub3(x2, x1);
   const V3x2 cr = cross3(e1, e2, one);
   const f2 mag = magnitude3(cr, one);
@@ -89,13 +73,9 @@ __device__ __forceinline__ void face_terms2(V3x2 x0, V3x2 x1, V3x2 x2, V3x2 v0, 
   const V3x2 D{add_p2(lift.x, drag.x, one), add_p2(lift.y, drag.y, one), add_p2(lift.z, drag.z, one)};
   const f2 a0 = angle_pos2(mag, dot3(e2, e1, one), one);
   const f2 a1 = angle_pos2(mag, neg2(dot3(e1, e3, one)), one);
-  bool okw = true;
-  f2 w0 = div_const2(a0, kPiF32, kRcpPi, okw), w1 = div_const2(a1, kPiF32, kRcpPi, okw);
-  if (!okw) {
-    w0 = div2_ieee_cold(a0, kPiF32);
-    w1 = div2_ieee_cold(a1, kPiF32);
-  }
-  const f2 w2 = sub2(sub2(dup2(1.0f), w0), w1);  // (1 - w0) - w1
+  const f2 rpi = dup2(kRcpPi), mone = neg2(one);
+  const f2 w0 = mul2(a0, rpi), w1 = mul2(a1, rpi);
+  const f2 w2 = fma2(w1, mone, fma2(w0, mone, dup2(1.0f)));  // (1 - w0) - w1, the products kept rounded
   const float2 dx = upk(D.x), dy = upk(D.y), dz = upk(D.z), u0 = upk(w0), u1 = upk(w1), u2 = upk(w2);
   DwA = make_float4(dx.x, dy.x, dz.x, u0.x);
   DwB = make_float4(dx.y, dy.y, dz.y, u0.y);

@@ -26,11 +26,15 @@ __device__ __forceinline__ void strut_forces(V3<T> p0, V3<T> p1, V3<T> v0, V3<T>
   df = (c * dot(v1 - v0, u)) * u;
 }
 
-// drag + lift of one face (springy_mesh.rs:634-646).
+// drag + lift of one face (springy_mesh.rs:634-646).  The f32 step takes
+// the mean velocity as the sum times RN(1/3) (the reference divides by 3: at
+// most an ulp apart, in the face terms only); the FP64 rerun divides.
 template <class T>
 __device__ __forceinline__ V3<T> face_total_force(V3<T> x0, V3<T> x1, V3<T> x2, V3<T> v0, V3<T> v1, V3<T> v2,
                                                   V3<T> wind, T neg_cd, T neg_cl) {
-  const V3<T> avg = ((v0 + v1) + v2) / T(3);
+  V3<T> avg;
+  if constexpr (sizeof(T) == 8) avg = ((v0 + v1) + v2) / T(3);
+  else avg = ((v0 + v1) + v2) * kRcp3;
   const V3<T> rv = avg - wind;
   const V3<T> cr = cross(x1 - x0, x2 - x0);
   const T area = magnitude(cr) / T(2);
@@ -47,14 +51,14 @@ __device__ __forceinline__ V3<T> face_total_force(V3<T> x0, V3<T> x1, V3<T> x2, 
 // step saves work the reference repeats: |a x b| is twice the face's area at
 // every corner, so corners 0 and 1 take the one magnitude
 // |(x1 - x0) x (x2 - x0)| the drag already needs, with their own dot products
-// in the reference's order; and the angles sum to pi, so corner 2's share is
-// (1 - w0) - w1.  Both differ from the reference's per-corner recomputation
-// by rounding only (about 1e-7 of the face's force), like the angle's own
-// last bits.
+// in the reference's order; the angles sum to pi, so corner 2's share is
+// (1 - w0) - w1; and a share is the angle times RN(1/pi) instead of over pi.
+// Each differs from the reference's per-corner computation by rounding only
+// (about 1e-7 of the face's force), like the angle's own last bits.
 template <class T>
 __device__ __forceinline__ T corner_share(V3<T> x0, V3<T> x1, V3<T> x2, T y, int k) {
   const T x = k == 0 ? dot(x2 - x0, x1 - x0) : dot(x0 - x1, x2 - x1);
-  return angle_of(y, x) / T(kPiF32);
+  return angle_of(y, x) * kRcpPi;
 }
 template <class T>
 __device__ __forceinline__ T face_corner_weight(V3<T> x0, V3<T> x1, V3<T> x2, int k) {

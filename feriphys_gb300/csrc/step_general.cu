@@ -132,9 +132,11 @@ __device__ __forceinline__ void flag_nonfinite(bool bad, unsigned* flags) {
 }
 
 // Fused Simulation::step for one mesh (accumulate -> integrate -> collide ->
-// pin restore -> clear), one thread per vertex.
+// pin restore -> clear), one thread per vertex.  The f32 form asks for 4
+// blocks of 256 per SM (at most 64 registers: the gather is latency-bound, so
+// resident warps count); the FP64 rerun keeps the registers it needs.
 template <class T, int FORM>
-__global__ void __launch_bounds__(256) k_step_general(int n, const Vec4<T>* __restrict__ pos,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_step_general(int n, const Vec4<T>* __restrict__ pos,
                                                       const Vec4<T>* __restrict__ vel,
                                                       const Vec4<T>* __restrict__ force_in,
                                                       Vec4<T>* __restrict__ pos_out, Vec4<T>* __restrict__ vel_out,
