@@ -215,22 +215,6 @@ __device__ __forceinline__ void collision_response(const ObsFace* __restrict__ F
   nv = vrn + vrt;
 }
 
-// First hit over the flattened obstacle faces, then the response.  Returns
-// true when the point collided.
-template <class T>
-__device__ __forceinline__ bool collide_point_all(const ObsFace* __restrict__ faces, int n_faces, V3<T> op, V3<T> ov,
-                                                  V3<T> oF, T om, V3<T>& np, V3<T>& nv, const StepConsts& c) {
-  const T dtd = T(c.dt_duration);
-  for (int f = 0; f < n_faces; ++f) {
-    T d_old, d_new;
-    if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
-      collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
-      return true;
-    }
-  }
-  return false;
-}
-
 // Margin of the query box: the computed crossing point can leave the
 // segment's box by a few ulps of the step and of the coordinates.  The
 // margin 1e-5 |a - b| + 1e-5 max(|a|, |b|) covers that many times over;
@@ -238,27 +222,6 @@ __device__ __forceinline__ bool collide_point_all(const ObsFace* __restrict__ fa
 // in fewer operations (a larger box only adds candidates).
 __device__ __forceinline__ float query_slack(float a, float b) {
   return 3.0001e-5f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f;
-}
-
-template <class T>
-__device__ __forceinline__ bool test_faces_from(const ObsFace* __restrict__ faces, const int* __restrict__ list_a,
-                                                int ba, int ea, const int* __restrict__ list_b, int bb, int eb,
-                                                V3<T> op, V3<T> ov, V3<T> oF, T om, V3<T>& np, V3<T>& nv,
-                                                const StepConsts& c) {
-  // visit the union of two ascending lists in ascending order
-  const T dtd = T(c.dt_duration);
-  while (ba < ea || bb < eb) {
-    const int fa = ba < ea ? list_a[ba] : 0x7fffffff;
-    const int fb = bb < eb ? list_b[bb] : 0x7fffffff;
-    int f;
-    if (fa <= fb) { f = fa; ++ba; } else { f = fb; ++bb; }
-    T d_old, d_new;
-    if (face_hit(faces + f, op, np, dtd, d_old, d_new)) {
-      collision_response(faces + f, d_old, d_new, op, ov, oF, om, T(c.dt), T(c.restitution), T(c.friction), np, nv);
-      return true;
-    }
-  }
-  return false;
 }
 
 // First hit with the broad phase: obstacles in order; within one, the faces
