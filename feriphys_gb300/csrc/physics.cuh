@@ -76,7 +76,10 @@ __device__ __forceinline__ T face_corner_weight(V3<T> x0, V3<T> x1, V3<T> x2, in
 }
 
 // F / m componentwise, exactly as IEEE division; the f32 form shares one
-// correctly rounded reciprocal of m (fastdiv.cuh).
+// correctly rounded reciprocal of m (fastdiv.cuh) and checks the three
+// quotients with one guard.  A zero component (a flat cloth's out-of-plane
+// force) is exactly a * RN(1/m), a zero of the right sign, and needs no
+// slow path; Markstein's correction would turn -0 into +0.
 struct MassDiv {
   float m, y;
   bool fast;
@@ -86,9 +89,25 @@ __device__ __forceinline__ MassDiv mass_div(float m) {
   return {m, fast ? rcp_rn_fast(m) : 0.0f, fast};
 }
 static __device__ __noinline__ V3<float> div3_ieee_cold(V3<float> F, float m) { return F / m; }
+// 2^-100 <= |x| <= 2^100 (the range div_known_rcp's fast path accepts)
+__device__ __forceinline__ bool markstein_range(float x) {
+  return ((__float_as_uint(x) & 0x7fffffffu) - 0x0d800000u) <= (0x71800000u - 0x0d800000u);
+}
+__device__ __forceinline__ float div_known_rcp_z(float a, float b, float y, bool& ok) {
+  const float q = __fmul_rn(a, y);
+  const float r = __fmaf_rn(-b, q, a);
+  const float q2 = __fmaf_rn(r, y, q);
+  const bool zero = a == 0.0f;
+  ok = ok && (zero || (markstein_range(a) && markstein_range(q2)));
+  return zero ? q : q2;
+}
 __device__ __forceinline__ V3<float> div_mass(V3<float> F, float m, const MassDiv& d) {
-  if (d.fast && m == d.m && !signbit(m) == !signbit(d.m))
-    return {div_known_rcp(F.x, d.m, d.y), div_known_rcp(F.y, d.m, d.y), div_known_rcp(F.z, d.m, d.y)};
+  if (d.fast && m == d.m) {
+    bool ok = true;
+    const V3<float> q{div_known_rcp_z(F.x, m, d.y, ok), div_known_rcp_z(F.y, m, d.y, ok),
+                      div_known_rcp_z(F.z, m, d.y, ok)};
+    if (ok) return q;
+  }
   return div3_ieee_cold(F, m);
 }
 struct MassDivD {

@@ -3,7 +3,8 @@
 * The correctly rounded division by a known reciprocal
   (feriphys_gb300/csrc/fastdiv.cuh) returns exactly the IEEE quotient: for
   every one of the 2^32 float numerators with the divisors 3 and pi, and for
-  2^30 random (numerator, divisor) pairs as in the F/m of the integration.
+  2^30 random (numerator, divisor) pairs, also through the integration's
+  grouped F/m (physics.cuh: div_mass) with signed zero numerators mixed in.
 * The branch-free reciprocals (fastdiv.cuh) equal the IEEE 1/x: rcp_rn_fast
   for every float of magnitude [2^-124, 2^124), rcp_of_root and its packed
   form for the square root of every float.
@@ -57,6 +58,12 @@ __global__ void random_pairs(unsigned long long n, unsigned long long* bad) {
     const float ref = __fdiv_rn(a, b);
     const float got = rcp_usable(b) ? div_known_rcp(a, b, __frcp_rn(b)) : __fdiv_rn(a, b);
     if (!same(got, ref)) ++local;
+    // the integration's grouped form (physics.cuh: div_mass), also for signed
+    // zero numerators, which it answers without the IEEE fallback
+    const float az = (i & 15) == 3 ? ((i & 16) ? -0.0f : 0.0f) : a;
+    const V3<float> F{az, a, -a};
+    const V3<float> q = div_mass(F, b, mass_div(b));
+    if (!same(q.x, __fdiv_rn(az, b)) || !same(q.y, ref) || !same(q.z, __fdiv_rn(-a, b))) ++local;
   }
   if (local) atomicAdd(bad, local);
 }
