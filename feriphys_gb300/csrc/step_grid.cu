@@ -516,6 +516,11 @@ __global__ void __launch_bounds__(TW * TH + HALO, TileGeom<TW, TH>::MIN_CTAS) k_
                                                                    const CUtensorMap* __restrict__ maps,
                                                                    const int* __restrict__ n_work_dev) {
   __shared__ int s_item;
+  // the current item's cloth descriptor, staged once per item: read from
+  // shared memory where the tile uses it, instead of held in registers
+  // (pointers and wind) across the whole tile
+  __shared__ ClothDesc s_d;
+  __shared__ int4 s_w;
   if (n_work_dev) n_work = *n_work_dev;  // a count made on the device (persistent mode)
   __shared__ uint64_t bar;
   uint32_t phase = 0;
@@ -540,9 +545,15 @@ __global__ void __launch_bounds__(TW * TH + HALO, TileGeom<TW, TH>::MIN_CTAS) k_
       __syncthreads();
     }
     if (item >= n_work) break;
-    const int4 w = work[item];
-    const ClothDesc& d = cloths[w.x];
+    if (threadIdx.x == 0) {
+      s_w = work[item];
+      s_d = cloths[s_w.x];
+    }
+    __syncthreads();  // also: every thread has finished the previous tile
+    const int4 w = s_w;
+    const ClothDesc& d = s_d;
     if (d.skip) {  // masked out: uniform over the CTA
+      __syncthreads();  // s_d is rewritten for the next item
       if (!persistent) break;
       continue;
     }
