@@ -511,7 +511,8 @@ int capture_checked_step(fgb_surrogate* g, fgb_sim* s, const Rollout& ro, int pa
     if ((e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault)) != cudaSuccess) break;
     if ((e = S::launch_set_fallback(h, g->d_counts, g->d_total, st)) != cudaSuccess) break;
     if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) break;
-    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // the other members zero
+    cudaGraphNodeParams cp{};  // every member zero
+    cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
     cp.conditional.type = cudaGraphCondTypeIf;
     cp.conditional.size = 1;

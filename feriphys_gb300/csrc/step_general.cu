@@ -89,7 +89,7 @@ __device__ __forceinline__ V3<T> gather_forces(int v, V3<T> P, V3<T> V, V3<T> F,
                                                const StepConsts& c) {
   const int s_beg = t.strut_off[v], s_end = t.strut_off[v + 1];
   const V3<T> wind{T(c.wind[0]), T(c.wind[1]), T(c.wind[2])};
-  if (FORM != 0) {
+  if constexpr (FORM != 0) {
     int own = t.own_off[v];  // owner position of v's next role-0 strut
     for (int e = s_beg; e < s_end; ++e) {
       int off, rank, role;
@@ -111,18 +111,18 @@ __device__ __forceinline__ V3<T> gather_forces(int v, V3<T> P, V3<T> V, V3<T> F,
                 i2 = corner == 2 ? v : u2;
       add_face<T>(F, i0, i1, i2, corner, pos, vel, wind, c);
     }
-    return F;
-  }
-  for (int e = s_beg; e < s_end; ++e) {
-    const int2 inc = t.strut_inc[e];
-    const float4 kcl = t.strut_kcl[inc.y >> 1];
-    add_strut<T>(F, P, V, xyz<T>(pos[inc.x]), xyz<T>(vel[inc.x]), inc.y & 1, kcl.x, kcl.y, kcl.z);
-  }
-  const int f_beg = t.face_off[v], f_end = t.face_off[v + 1];
-  for (int e = f_beg; e < f_end; ++e) {
-    const int fc = t.face_inc[e];
-    const int4 fv = t.face_vtx[fc >> 2];
-    add_face<T>(F, fv.x, fv.y, fv.z, fc & 3, pos, vel, wind, c);
+  } else {
+    for (int e = s_beg; e < s_end; ++e) {
+      const int2 inc = t.strut_inc[e];
+      const float4 kcl = t.strut_kcl[inc.y >> 1];
+      add_strut<T>(F, P, V, xyz<T>(pos[inc.x]), xyz<T>(vel[inc.x]), inc.y & 1, kcl.x, kcl.y, kcl.z);
+    }
+    const int f_beg = t.face_off[v], f_end = t.face_off[v + 1];
+    for (int e = f_beg; e < f_end; ++e) {
+      const int fc = t.face_inc[e];
+      const int4 fv = t.face_vtx[fc >> 2];
+      add_face<T>(F, fv.x, fv.y, fv.z, fc & 3, pos, vel, wind, c);
+    }
   }
   return F;
 }

@@ -118,22 +118,6 @@ __global__ void __launch_bounds__(256) k_step_grid_v1(int R, int C, const float4
 template <int TW, int TH>
 struct TileGeom {
   static constexpr int EW = TW + 4, EH = TH + 4;  // staged region, origin (r0-2, c0-2)
-  // strut owner regions (row range x col range relative to (r0, c0))
-  static constexpr int KH_W = TW + 1, KH_H = TH;      // rows [0, TH), cols [-1, TW)
-  static constexpr int KV_W = TW, KV_H = TH + 1;      // rows [-1, TH), cols [0, TW)
-  static constexpr int KS_W = TW + 1, KS_H = TH + 1;  // rows [-1, TH), cols [-1, TW)
-  static constexpr int KBH_W = TW + 2, KBH_H = TH;    // rows [0, TH), cols [-2, TW)
-  static constexpr int KBV_W = TW, KBV_H = TH + 2;    // rows [-2, TH), cols [0, TW)
-  static constexpr int Q_W = TW + 1, Q_H = TH + 1;    // quads rows [-1, TH), cols [-1, TW)
-  static constexpr int N_KH = KH_W * KH_H, N_KV = KV_W * KV_H, N_KS = KS_W * KS_H;
-  static constexpr int N_TRI = N_KH + N_KV + N_KS;
-  static constexpr int N_KBH = KBH_W * KBH_H, N_KBV = KBV_W * KBV_H;
-  static constexpr int N_BIND = N_KBH + N_KBV;
-  static constexpr int N_Q = Q_W * Q_H;
-  // buffer in float4 units: struts need 2 (spring, damper), a quad needs
-  // 2 float4 + 2 float2 = 3 float4
-  static constexpr int BUF = (2 * N_TRI > 2 * N_BIND ? (2 * N_TRI > 3 * N_Q ? 2 * N_TRI : 3 * N_Q)
-                                                     : (2 * N_BIND > 3 * N_Q ? 2 * N_BIND : 3 * N_Q));
   // resident CTAs per SM the launch bounds ask for: 64 registers per thread
   // at TW * TH + 64 threads (32x4: 5, 32x8: 3, 32x12: 2 with 72 registers)
   static constexpr int MIN_CTAS = TH <= 4 ? 5 : (TH <= 8 ? 3 : 2);
@@ -581,14 +565,6 @@ size_t tiled_smem_bytes_t() {
   using G = TileGeom<kTileW, TH>;
   using I = Interior<kTileW, TH>;
   return 2 * sizeof(float4) * G::EH * G::EW + size_t(I::BYTES);
-}
-
-size_t tiled_smem_bytes(int th) {
-  switch (th) {
-    case 4: return tiled_smem_bytes_t<4>();
-    case 12: return tiled_smem_bytes_t<12>();
-    default: return tiled_smem_bytes_t<8>();
-  }
 }
 
 // Tensor map of one float4 state array of an R x C grid, seen as R rows of
