@@ -77,6 +77,11 @@ bool batch_tile_height_ok(int th);
 // Tiles of one cloth for the batch work list: {cloth, tile x, tile y, interior}.
 void batch_tiles(int cloth, int rows, int cols, int th, int* out4 /* may be null */, int* n_ring, int* n_interior);
 
+// The single-cloth tiled kernel's grid: the CTA count for an R x C cloth and
+// 32 x th tiles, and (out3 non-null) each CTA's {tile x, tile y, interior}
+// in blockIdx order, by the kernel's own mapping.
+int grid_tiles(int rows, int cols, int th, int* out3 /* may be null */);
+
 // mode 0: one CTA per work item; mode 1: persistent CTAs pulling items from
 // *counter (reset to 0 by the caller before the launch).
 // maps: null, or per cloth 4 tensor maps {pos[0], vel[0], pos[1], vel[1]}

@@ -196,7 +196,7 @@ struct TileSplit {
   int bx0, bx1, by0, by1;  // interior rectangle (empty when bx1 < bx0 or by1 < by0)
 };
 
-__device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, int& by) {
+__host__ __device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, int& by) {
   const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
   if (!has_interior) {
     bx = k % t.tx;
@@ -221,6 +221,20 @@ __device__ __forceinline__ void ring_tile(const TileSplit& t, int k, int& bx, in
   by = t.by0 + k / per_row;
   const int j = k % per_row;
   bx = j < t.bx0 ? j : t.bx1 + 1 + (j - t.bx0);
+}
+
+// Tile of CTA b of the single-cloth kernel: the first n_ring CTAs take the
+// ring tiles in ring_tile's order, the rest the interior rectangle row by
+// row.  Returns whether the tile is an interior one.
+__host__ __device__ __forceinline__ bool grid_tile(const TileSplit& t, int n_ring, int b, int& bx, int& by) {
+  if (b < n_ring) {
+    ring_tile(t, b, bx, by);
+    return false;
+  }
+  const int k = b - n_ring, nbx = t.bx1 - t.bx0 + 1;
+  bx = t.bx0 + k % nbx;
+  by = t.by0 + k / nbx;
+  return true;
 }
 
 // One tile of one cloth.  No early return: the batched kernel runs it in a
@@ -475,17 +489,13 @@ __global__ void __launch_bounds__(TW * TH + HALO, TileGeom<TW, TH>::MIN_CTAS) k_
     tc::mbar_init(&bar, 1);
     tc::mbar_fence_init();
   }
-  if (b < n_ring) {
-    int bx, by;
-    ring_tile(split, b, bx, by);
+  int bx, by;
+  if (!grid_tile(split, n_ring, b, bx, by))
     tile_step<TW, TH, HALO, false, TMA>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
                                         V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv, &bar, 0);
-  } else {
-    const int k = b - n_ring, nbx = split.bx1 - split.bx0 + 1;
-    tile_step<TW, TH, HALO, true, TMA>(split.bx0 + k % nbx, split.by0 + k / nbx, R, C, planes, pos, vel,
-                                       force_in, pos_out, vel_out, c, V3<float>{c.wind[0], c.wind[1], c.wind[2]},
-                                       c.flags, mp, mv, &bar, 0);
-  }
+  else
+    tile_step<TW, TH, HALO, true, TMA>(bx, by, R, C, planes, pos, vel, force_in, pos_out, vel_out, c,
+                                       V3<float>{c.wind[0], c.wind[1], c.wind[2]}, c.flags, mp, mv, &bar, 0);
 }
 
 // Many cloths in one launch.  Work items {cloth, tile x, tile y, interior}
@@ -678,6 +688,16 @@ void batch_tiles(int cloth, int rows, int cols, int th, int* out4, int* n_ring, 
       out4[4 * k] = cloth; out4[4 * k + 1] = bx; out4[4 * k + 2] = by; out4[4 * k + 3] = 1;
       ++k;
     }
+}
+
+int grid_tiles(int rows, int cols, int th, int* out3) {
+  const TileSplit t = split_tiles(rows, cols, th);
+  const bool has_interior = t.bx1 >= t.bx0 && t.by1 >= t.by0;
+  const int n_interior = has_interior ? (t.bx1 - t.bx0 + 1) * (t.by1 - t.by0 + 1) : 0;
+  const int n_ring = t.tx * t.ty - n_interior;
+  for (int b = 0; out3 && b < n_ring + n_interior; ++b)  // blockIdx.x b of k_step_grid_tiled
+    out3[3 * b + 2] = grid_tile(t, n_ring, b, out3[3 * b], out3[3 * b + 1]) ? 1 : 0;
+  return n_ring + n_interior;
 }
 
 cudaError_t prime_step_kernels() {
