@@ -638,7 +638,7 @@ def run_surrogate(args, rank, world, dist, torch, fgb, W, emit=True):
             "fallbacks": fallbacks,
             "fallback_fraction": fallbacks / float(n_cloths_eval * args.coarse_steps),
             "by_horizon": {str(k): v for k, v in horizon.items()},
-            "target": "north star: >= 5x the simulated seconds per second of the plain solver at <= 1e-2 relative "
+            "target": ">= 5x the simulated seconds per second of the plain solver at <= 1e-2 relative "
                       "position error after 1000 coarse steps; by_horizon gives the speed-up over the first c "
                       "coarse steps and the error after them",
             "simulated_seconds_per_s": {"surrogate": float(T) / (coarse_ms * 1e-3),
