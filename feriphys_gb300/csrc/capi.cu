@@ -109,7 +109,8 @@ P* mapped_host(P* p) {
 }
 
 int ensure_io(fgb_mesh* m, size_t bytes) {
-  if (m->d_io_bytes < bytes) {
+  if (m->d_io_bytes < bytes || !m->d_io) {
+    m->d_io_bytes = 0;  // a failed allocation leaves no buffer and no capacity
     FGB_CUDA(dalloc(m->d_io, bytes));
     m->d_io_bytes = bytes;
   }
@@ -448,20 +449,22 @@ int prepare_batch(fgb_sim* s) {
       fgb::batch_tiles(int(i), int(grid[i]->topo.rows), int(grid[i]->topo.cols), s->tile_h, work.data() + at, &nr,
                        &ni);
     }
-    s->n_work = int(work.size() / 4);
+    drop_graphs(s);  // before the buffers the graphs launch on are replaced
+    s->n_work = 0;
     FGB_CUDA(dalloc(s->d_work, work.size() * sizeof(int)));
     FGB_CUDA(cudaMemcpy(s->d_work, work.data(), work.size() * sizeof(int), cudaMemcpyHostToDevice));
+    s->n_work = int(work.size() / 4);
     s->work_host = work;
     if (!s->d_counter) FGB_CUDA(dalloc(s->d_counter, sizeof(int)));
-    drop_graphs(s);
     if (membership) s->mode = -1;
   }
   if (membership || reshape || desc.size() != s->desc.size() ||
       std::memcmp(desc.data(), s->desc.data(), desc.size() * sizeof(fgb::ClothDesc)) != 0) {
-    if (s->d_desc_cap < desc.size()) {
+    if (s->d_desc_cap < desc.size() || !s->d_desc) {
+      drop_graphs(s);
+      s->d_desc_cap = 0;
       FGB_CUDA(dalloc(s->d_desc, desc.size() * sizeof(fgb::ClothDesc)));
       s->d_desc_cap = desc.size();
-      drop_graphs(s);
     }
     FGB_CUDA(cudaMemcpyAsync(s->d_desc, desc.data(), desc.size() * sizeof(fgb::ClothDesc), cudaMemcpyHostToDevice,
                              bs));
@@ -472,10 +475,11 @@ int prepare_batch(fgb_sim* s) {
     for (size_t i = 0; i < desc.size() && maps_ok; ++i)
       maps_ok = fgb::encode_cloth_maps(desc[i], s->tile_h, mp + i * fgb::kClothMapBytes);
     if (maps_ok) {
-      if (s->d_maps_cap < desc.size()) {
+      if (s->d_maps_cap < desc.size() || !s->d_maps) {
+        drop_graphs(s);
+        s->d_maps_cap = 0;
         FGB_CUDA(dalloc(s->d_maps, desc.size() * fgb::kClothMapBytes));
         s->d_maps_cap = desc.size();
-        drop_graphs(s);
       }
       FGB_CUDA(cudaMemcpyAsync(s->d_maps, mp, desc.size() * fgb::kClothMapBytes, cudaMemcpyHostToDevice, bs));
     } else {
