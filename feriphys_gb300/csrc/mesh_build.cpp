@@ -258,7 +258,7 @@ int build_cloth(uint64_t rows, uint64_t cols, float spacing, const float positio
     err = "Cloth::new needs rows >= 2 and cols >= 2";
     return FGB_EINVAL;
   }
-  if (rows * cols > 0x7fffffffull) {
+  if (rows > 0x7fffffffull || cols > 0x7fffffffull || rows * cols > 0x7fffffffull) {  // no 64-bit wrap
     err = "cloth too large";
     return FGB_EINVAL;
   }

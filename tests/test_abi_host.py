@@ -123,6 +123,11 @@ def test_error_codes(fgb):
     with pytest.raises(fgb.FgbError) as e:
         fgb.Cloth.new(1, 4, 0.1, (0, 0, 0), 0.01, 1, 1, 1, 1, 1, 1)
     assert e.value.code == -1
+    # more than 2^31 - 1 vertices, including a product that wraps to 0 in 64 bits
+    for rows, cols in ((1 << 16, 1 << 16), (1 << 32, 1 << 32), (2, 1 << 40)):
+        with pytest.raises(fgb.FgbError) as e:
+            fgb.Cloth.new(rows, cols, 0.1, (0, 0, 0), 0.01, 1, 1, 1, 1, 1, 1)
+        assert e.value.code == -1
     m = fgb.SpringyMesh.new([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [0, 1, 2], 1.0, 1.0, 1.0)
     with pytest.raises(fgb.FgbError) as e:
         m.add_pin(3)
