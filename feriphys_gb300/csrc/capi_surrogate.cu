@@ -911,7 +911,8 @@ int fgb_surrogate_dataset_info(const fgb_surrogate* g, uint64_t out[2]) {
 
 int fgb_surrogate_dataset_get(fgb_surrogate* g, uint64_t first, uint64_t n, float* feat, float* tgt) {
   if (!g) return fail(FGB_EINVAL, "null surrogate");
-  if (first + n > uint64_t(g->count)) return fail(FGB_EINDEX, "rows beyond the dataset");
+  const uint64_t count = uint64_t(g->count);
+  if (first > count || n > count - first) return fail(FGB_EINDEX, "rows beyond the dataset");
   if (n == 0) return FGB_OK;
   std::vector<float> F(n * S::kRawStride), Tt(n * 4);
   FGB_CUDA(cudaMemcpy(F.data(), g->d_feat + first * S::kRawStride, F.size() * sizeof(float), cudaMemcpyDeviceToHost));

@@ -164,6 +164,10 @@ def test_collect_matches_oracle_and_normalization():
         tref = (vel1[:, :3] - vel[:, :3]) * s
         assert np.allclose(t, tref, rtol=1e-6, atol=1e-7)
     assert sur.dataset_info() == (2 * n, 10 * n)
+    for first, rows in ((2 * n, 1), ((1 << 64) - 1, 2)):  # past the end; an end that wraps in 64 bits
+        with pytest.raises(fgb.FgbError) as e:
+            sur.dataset(first, rows)
+        assert e.value.code == -2
     sur.fit_normalization()
     f, t = sur.dataset(0, 2 * n)
     m, sd, om, osd = sur.get_normalization()
