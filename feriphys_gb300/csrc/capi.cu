@@ -1203,6 +1203,15 @@ int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const*
   FGB_CHECK_RC(make_obstacle_faces(obstacles, n_obstacles, faces));
   for (uint64_t i = 0; i < n_meshes; ++i)
     if (!meshes[i]) return fail(FGB_EINVAL, "null mesh");
+  // the reference's Simulation owns its meshes (a Vec<SpringyMesh>), so none
+  // appears twice; a repeated handle would be stepped twice per step by the
+  // one-mesh path and once by the batched one
+  {
+    std::set<const fgb_mesh*> seen;
+    for (uint64_t i = 0; i < n_meshes; ++i)
+      if (!seen.insert(meshes[i]).second)
+        return fail(FGB_EINVAL, "mesh " + std::to_string(i) + " appears twice in the simulation's mesh list");
+  }
   // one simulation steps its meshes with one kernel per step on one device:
   // meshes created on different devices cannot share it
   for (uint64_t i = 1; i < n_meshes; ++i)

@@ -209,7 +209,8 @@ int fgb_collidable_destroy(fgb_obstacle* o);
  * step it only while they live.  fgb_sim_destroy never touches them, so the
  * handles may be destroyed in any order.  Every mesh must have been created
  * with the same CUDA device current (a mesh belongs to the device current at
- * its creation); meshes of different devices give FGB_EINVAL. */
+ * its creation); meshes of different devices give FGB_EINVAL, and so does
+ * a mesh listed twice (the reference's Simulation owns each mesh once). */
 int fgb_sim_new(fgb_mesh* const* meshes, uint64_t n_meshes, fgb_obstacle* const* obstacles, uint64_t n_obstacles,
                 fgb_sim** out);
 

@@ -138,6 +138,9 @@ def test_error_codes(fgb):
     with pytest.raises(fgb.FgbError) as e:
         fgb.CollidableMesh.new([[0, 0, 0], [1, 0, 0]], [0, 0, 1])
     assert e.value.code == -1
+    with pytest.raises(fgb.FgbError) as e:  # one mesh twice in one simulation
+        fgb.Simulation.new([m, m], [])
+    assert e.value.code == -1
     sim = fgb.Simulation.new([m], [])
     for bad in (-1.0, float("nan"), float("inf")):
         with pytest.raises(fgb.FgbError) as e:
