@@ -216,6 +216,19 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
+def _out_array(out, shape, dtype=np.float32):
+    """A caller's output buffer as the library writes it (a pinned one by the
+    GPU directly): exactly the expected dtype and size, C-contiguous and
+    writeable; a fresh array when ``out`` is None."""
+    size = int(np.prod(shape))
+    if out is None:
+        return np.empty(shape, dtype)
+    if (not isinstance(out, np.ndarray) or out.dtype != dtype or out.size != size or not out.flags.c_contiguous
+            or not out.flags.writeable):
+        raise ValueError("out must be a writeable C-contiguous %s array of %d elements" % (np.dtype(dtype).name, size))
+    return out
+
+
 def _f32(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1))
 
@@ -300,9 +313,7 @@ class SpringyMesh:
 
     def get_points(self, out=None) -> np.ndarray:
         """Points as [n, 10] float32 in the Stateful::as_state layout."""
-        n = self.n_points
-        if out is None:
-            out = np.empty((n, 10), np.float32)
+        out = _out_array(out, (self.n_points, 10))
         _check(_lib().fgb_mesh_get_points(self._h, _ptr(out)))
         return out
 
@@ -320,8 +331,7 @@ class SpringyMesh:
 
     def get_positions(self, out=None) -> np.ndarray:
         """Positions as [n, 3] float32 (a pinned ``out`` is written by the GPU directly)."""
-        if out is None:
-            out = np.empty((self.n_points, 3), np.float32)
+        out = _out_array(out, (self.n_points, 3))
         _check(_lib().fgb_mesh_get_positions(self._h, _ptr(out)))
         return out
 

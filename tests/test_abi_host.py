@@ -165,6 +165,22 @@ def test_collidable_counts_match_oracle(fgb, orc):
     assert fgb.CollidableMesh.new(pos, idx).counts() == orc.CollidableMesh(pos, idx).counts()
 
 
+def test_output_buffers_are_checked_before_the_library_writes(fgb):
+    m = fgb.SpringyMesh.new([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [0, 1, 2], 1.0, 1.0, 1.0)
+    wrong = (np.empty((2, 10), np.float32), np.empty((3, 10), np.float64), np.empty((10, 3), np.float32).T,
+             np.empty((3, 10), np.float32)[:, ::-1], [[0.0] * 10] * 3)
+    for out in wrong:
+        with pytest.raises(ValueError):
+            m.get_points(out=out)
+    ro = np.empty((3, 10), np.float32)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        m.get_points(out=ro)
+    for out in (np.empty((4, 3), np.float32), np.empty((3, 3), np.int32)):
+        with pytest.raises(ValueError):
+            m.get_positions(out=out)
+
+
 def test_points_round_trip_host(fgb):
     m = fgb.SpringyMesh.new([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [0, 1, 2], 3.0, 1.0, 1.0)
     p = m.get_points()
