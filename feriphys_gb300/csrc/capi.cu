@@ -570,7 +570,10 @@ int tune_batch(fgb_sim* s) {
   int best_mode = modes[0], best_h = heights[0];
   cudaEvent_t a, b;
   FGB_CUDA(cudaEventCreate(&a));
-  FGB_CUDA(cudaEventCreate(&b));
+  if (const cudaError_t e = cudaEventCreate(&b); e != cudaSuccess) {
+    cudaEventDestroy(a);
+    return fail(FGB_ECUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
+  }
   int rc = FGB_OK;
   for (int th : heights) {
     for (int mode : modes) {
